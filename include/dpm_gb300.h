@@ -1,0 +1,177 @@
+/*
+ * dpm_gb300 -- C ABI of the GB300 (sm_103a) Deformable Particle Model step.
+ *
+ * This is the drop-in boundary beneath the clDPM Python module
+ * (Cell2D/Tissue2D/Cell3D/Tissue3D).  It replaces the OpenCL buffers,
+ * program build and kernel enqueues inside the reference's step loops:
+ *
+ *   Tissue2D::CLEulerUpdate   src/Tissue2D.cpp:116-241
+ *   Tissue3D::CLEulerUpdate   src/Tissue3D.cpp:118-522
+ *
+ * and the kernels they enqueue (shaders/Cell2D_kernel.cl,
+ * shaders/Cell3D_Kernel.cl).  Reference lines for each entry point are given
+ * beside it.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a DPM_E* code; the message of the
+ *    last failure on the calling thread is returned by dpm_last_error().
+ *  - All pointers in signatures are HOST pointers owned by the caller, except
+ *    where a name says "_dev".  Device state is owned by the object.
+ *  - A context owns one CUDA stream; objects created from it run on that
+ *    stream.  An object is not re-entrant; distinct contexts may be used from
+ *    distinct threads.
+ *  - 2D vertex data are ragged and cell-major: cell c's vertex v is at
+ *    xy[2*(first(c)+v)], first(c) = sum of nv over the cells before c.
+ *    3D vertex data are cell-major with one face table for all cells:
+ *    xyz[3*(c*nv+v)].
+ *  - A "batch" holds one or more independent tissues that step together;
+ *    a batch of one tissue is the plain single-system path.
+ */
+#ifndef DPM_GB300_H
+#define DPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPM_OK 0
+#define DPM_EINVAL 1    /* bad argument (std::invalid_argument in the reference) */
+#define DPM_ECUDA 2     /* CUDA runtime failure */
+#define DPM_ECAPACITY 3 /* size beyond a documented limit */
+#define DPM_ENONFINITE 4 /* non-finite vertex positions after stepping */
+#define DPM_ESTATE 5    /* call out of order (e.g. step before upload) */
+
+typedef struct dpm_ctx dpm_ctx;
+typedef struct dpm2d_batch dpm2d_batch;
+typedef struct dpm3d_batch dpm3d_batch;
+
+/* Last error message of the calling thread ("" if none). */
+const char *dpm_last_error(void);
+
+/* Library version string. */
+const char *dpm_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* Context: device + stream.  Replaces the per-object cl::Platform/Device/  */
+/* Context/CommandQueue (src/Tissue2D.cpp:35-37, 213; src/Tissue3D.cpp:32-34,*/
+/* 362).                                                                    */
+/* ---------------------------------------------------------------------- */
+int dpm_ctx_create(int device, dpm_ctx **out);
+int dpm_ctx_destroy(dpm_ctx *ctx);
+int dpm_ctx_synchronize(dpm_ctx *ctx);
+/* Number of SMs of the context's device (for schedulers and tuners). */
+int dpm_ctx_sm_count(dpm_ctx *ctx, int *out);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work (timing events, copies) with the library's. */
+int dpm_ctx_stream(dpm_ctx *ctx, void **stream);
+
+/* ---------------------------------------------------------------------- */
+/* 2D batches                                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Creates a batch of ntissues tissues; tissue t has ncells[t] cells and the
+ * cells (in tissue order) have nv[] vertices each (3 <= nv <= 256).
+ * Replaces the buffer sizing of src/Tissue2D.cpp:117-140, 149-168. */
+int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells,
+                 const unsigned *nv, dpm2d_batch **out);
+int dpm2d_destroy(dpm2d_batch *b);
+
+/* Per-cell constants, one value per cell in batch order: Ka, Kl, Kb, a0, l0,
+ * r0 (the fields of DPM::Cell2D the kernels read, src/Tissue2D.cpp:129-136).
+ */
+int dpm2d_set_cells(dpm2d_batch *b, const float *Ka, const float *Kl,
+                    const float *Kb, const float *a0, const float *l0,
+                    const float *r0);
+
+/* Per-tissue constants, one value per tissue: box size L, repulsion Kre,
+ * attraction Kat, periodic flag pbc (the kernel arguments set at
+ * src/Tissue2D.cpp:195-205). */
+int dpm2d_set_tissues(dpm2d_batch *b, const float *L, const float *Kre,
+                      const float *Kat, const int *pbc);
+
+/* Vertex positions in (host, float[2*total]); returns after the copy and
+ * the initial geometry are complete.  Replaces the COPY_HOST_PTR upload of
+ * src/Tissue2D.cpp:149-151. */
+int dpm2d_upload(dpm2d_batch *b, const float *xy);
+
+/* Runs nsteps overdamped Euler steps of size dt on every tissue.  Replaces
+ * the step loop of src/Tissue2D.cpp:215-229 (area, perimeter, bending,
+ * attraction and repulsion forces, then x += F*dt). */
+int dpm2d_step(dpm2d_batch *b, int nsteps, float dt);
+
+/* Positions and the forces of the last step (host float[2*total] each; F may
+ * be NULL).  Replaces the read-backs of src/Tissue2D.cpp:223-233. */
+int dpm2d_download(dpm2d_batch *b, float *xy, float *F);
+
+/* Totals of a batch: cells and vertices. */
+int dpm2d_sizes(dpm2d_batch *b, int *ncells, long *nvertices);
+
+/* Tuning knobs (0 keeps the current value): neighbour-list rebuild period
+ * in steps (even) and skin distance relative to the mean cell radius. */
+int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel,
+                     int warps_per_block);
+
+/* Diagnostics: per-vertex containment flags of the last step (uint8 per
+ * vertex; 1 = inside another cell, the reference's `overlaps`), per-cell
+ * area (float), and counts of neighbour-list rebuilds / brute-force steps. */
+int dpm2d_last_contained(dpm2d_batch *b, unsigned char *flags);
+int dpm2d_cell_areas(dpm2d_batch *b, float *area);
+int dpm2d_stats(dpm2d_batch *b, long *rebuilds, long *fallback_steps);
+
+/* Cell-list snapshot for host verification (see dpm2d_rebuild_now):
+ * sorted bin keys and cell ids (uint32[ncells] each), per-cell neighbour
+ * counts (int32[ncells]) and lists (int32[ncells*maxnb]). */
+int dpm2d_rebuild_now(dpm2d_batch *b);
+int dpm2d_cell_list(dpm2d_batch *b, unsigned *keys, unsigned *ids,
+                    int *nn, int *nbr, int *maxnb, float *geom);
+/* Bin layout of the last rebuild: bits of the local bin index in a key,
+ * and per tissue the bins per axis, bin width and skin. */
+int dpm2d_bins(dpm2d_batch *b, int *local_bits, int *nbins, float *binw,
+               float *skin);
+/* Enqueues exactly one launch of the fused step kernel on the context's
+ * stream (no rebuild; stale lists fall back to a tissue scan), without
+ * synchronizing.  For per-kernel timing and profiling. */
+int dpm2d_step_kernel(dpm2d_batch *b, float dt);
+
+/* ---------------------------------------------------------------------- */
+/* 3D batches                                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Creates a batch of 3D tissues whose cells all share the mesh topology
+ * faces[nf*3] over nv vertices (the reference uses cell 0's face table for
+ * every cell, src/Tissue3D.cpp:144-146).  nv <= 2562. */
+int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv,
+                 int nf, const unsigned *faces, dpm3d_batch **out);
+int dpm3d_destroy(dpm3d_batch *b);
+
+/* Per-cell constants (src/Tissue3D.cpp:172-178): Kv, Ka, Ks, v0, a0, l0.
+ * Kb (triangle bending) and adh (adhesion range; default 2*l0) are
+ * extensions and may be NULL. */
+int dpm3d_set_cells(dpm3d_batch *b, const float *Kv, const float *Ka,
+                    const float *Ks, const float *v0, const float *a0,
+                    const float *l0, const float *Kb, const float *adh);
+/* Per-tissue constants: L, Kre (the reference's Kc), pbc. */
+int dpm3d_set_tissues(dpm3d_batch *b, const float *L, const float *Kre,
+                      const int *pbc);
+int dpm3d_upload(dpm3d_batch *b, const float *xyz);
+/* Replaces the step loop of src/Tissue3D.cpp:372-445. */
+int dpm3d_step(dpm3d_batch *b, int nsteps, float dt);
+/* Forces are those of the last step (read after its Euler update,
+ * src/Tissue3D.cpp:425-434). */
+int dpm3d_download(dpm3d_batch *b, float *xyz, float *F);
+int dpm3d_sizes(dpm3d_batch *b, int *ncells, long *nvertices);
+/* Neighbour-list rebuild period (steps) and skin relative to the mean cell
+ * diameter (0 keeps the current value). */
+int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel);
+/* Per-vertex count of other cells whose winding number passed the
+ * reference's threshold in the last step (uint8 per vertex). */
+int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,318 @@
+"""ctypes binding of the C ABI (include/dpm_gb300.h).
+
+This is the same binding a Python caller of the library would write by hand;
+the tests and the benchmark go through it so that what they exercise is the
+C boundary itself.  Loading fails loudly when the native library is missing:
+there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libdpm_gb300.so")
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_uint_p = ctypes.POINTER(ctypes.c_uint)
+_c_float_p = ctypes.POINTER(ctypes.c_float)
+_c_long_p = ctypes.POINTER(ctypes.c_long)
+_c_ubyte_p = ctypes.POINTER(ctypes.c_ubyte)
+_vp = ctypes.c_void_p
+
+# name -> (restype, argtypes); the full exported surface of dpm_gb300.h
+SIGNATURES = {
+    "dpm_last_error": (ctypes.c_char_p, []),
+    "dpm_version": (ctypes.c_char_p, []),
+    "dpm_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
+    "dpm_ctx_destroy": (ctypes.c_int, [_vp]),
+    "dpm_ctx_synchronize": (ctypes.c_int, [_vp]),
+    "dpm_ctx_sm_count": (ctypes.c_int, [_vp, _c_int_p]),
+    "dpm_ctx_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "dpm2d_create": (ctypes.c_int, [_vp, ctypes.c_int, _c_int_p, _c_uint_p, ctypes.POINTER(_vp)]),
+    "dpm2d_destroy": (ctypes.c_int, [_vp]),
+    "dpm2d_set_cells": (ctypes.c_int, [_vp] + [_c_float_p] * 6),
+    "dpm2d_set_tissues": (ctypes.c_int, [_vp, _c_float_p, _c_float_p, _c_float_p, _c_int_p]),
+    "dpm2d_upload": (ctypes.c_int, [_vp, _vp]),
+    "dpm2d_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+    "dpm2d_download": (ctypes.c_int, [_vp, _vp, _vp]),
+    "dpm2d_sizes": (ctypes.c_int, [_vp, _c_int_p, _c_long_p]),
+    "dpm2d_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float, ctypes.c_int]),
+    "dpm2d_last_contained": (ctypes.c_int, [_vp, _c_ubyte_p]),
+    "dpm2d_cell_areas": (ctypes.c_int, [_vp, _c_float_p]),
+    "dpm2d_stats": (ctypes.c_int, [_vp, _c_long_p, _c_long_p]),
+    "dpm2d_rebuild_now": (ctypes.c_int, [_vp]),
+    "dpm2d_cell_list": (ctypes.c_int, [_vp, _c_uint_p, _c_uint_p, _c_int_p, _c_int_p, _c_int_p,
+                                       _c_float_p]),
+    "dpm2d_bins": (ctypes.c_int, [_vp, _c_int_p, _c_int_p, _c_float_p, _c_float_p]),
+    "dpm2d_step_kernel": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "dpm3d_create": (ctypes.c_int, [_vp, ctypes.c_int, _c_int_p, ctypes.c_int, ctypes.c_int,
+                                    _c_uint_p, ctypes.POINTER(_vp)]),
+    "dpm3d_destroy": (ctypes.c_int, [_vp]),
+    "dpm3d_set_cells": (ctypes.c_int, [_vp] + [_c_float_p] * 8),
+    "dpm3d_set_tissues": (ctypes.c_int, [_vp, _c_float_p, _c_float_p, _c_int_p]),
+    "dpm3d_upload": (ctypes.c_int, [_vp, _vp]),
+    "dpm3d_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+    "dpm3d_download": (ctypes.c_int, [_vp, _vp, _vp]),
+    "dpm3d_sizes": (ctypes.c_int, [_vp, _c_int_p, _c_long_p]),
+    "dpm3d_last_winding": (ctypes.c_int, [_vp, _c_ubyte_p]),
+    "dpm3d_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+}
+
+_lib = None
+
+
+class DPMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH, strict: bool = False):
+    """Loads the library and declares every entry point it exports.  With
+    strict=True a missing symbol raises."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        try:
+            fn = getattr(lib, name)
+        except AttributeError:
+            if strict:
+                raise
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc != 0:
+        msg = _lib.dpm_last_error().decode() if _lib is not None else ""
+        raise DPMError(rc, msg)
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(_c_float_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Context:
+    """dpm_ctx: one CUDA device and stream."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = _vp()
+        check(self.lib.dpm_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+
+    def sm_count(self) -> int:
+        n = ctypes.c_int()
+        check(self.lib.dpm_ctx_sm_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def synchronize(self):
+        check(self.lib.dpm_ctx_synchronize(self.h))
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        p = _vp()
+        check(self.lib.dpm_ctx_stream(self.h, ctypes.byref(p)))
+        return int(p.value or 0)
+
+    def close(self):
+        if self.h:
+            self.lib.dpm_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch2D:
+    """dpm2d_batch: independent 2D tissues stepped together."""
+
+    def __init__(self, ctx: Context, ncells, nv):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        nc = np.ascontiguousarray(ncells, dtype=np.int32)
+        self.nv = np.ascontiguousarray(nv, dtype=np.uint32)
+        h = _vp()
+        check(self.lib.dpm2d_create(ctx.h, len(nc), nc.ctypes.data_as(_c_int_p),
+                                    self.nv.ctypes.data_as(_c_uint_p), ctypes.byref(h)))
+        self.h = h
+        self.ntissues = len(nc)
+        self.ncells = int(nc.sum())
+        self.nverts = int(self.nv.sum())
+
+    def set_cells(self, Ka, Kl, Kb, a0, l0, r0):
+        arrs = [_f32(x) for x in (Ka, Kl, Kb, a0, l0, r0)]
+        for x in arrs:
+            if x.shape != (self.ncells,):
+                raise ValueError("per-cell arrays must have one value per cell")
+        check(self.lib.dpm2d_set_cells(self.h, *[fptr(x) for x in arrs]))
+
+    def set_tissues(self, L, Kre, Kat, pbc):
+        L, Kre, Kat = (_f32(np.broadcast_to(x, (self.ntissues,))) for x in (L, Kre, Kat))
+        p = np.ascontiguousarray(np.broadcast_to(pbc, (self.ntissues,)), dtype=np.int32)
+        check(self.lib.dpm2d_set_tissues(self.h, fptr(L), fptr(Kre), fptr(Kat),
+                                         p.ctypes.data_as(_c_int_p)))
+
+    def set_tuning(self, rebuild_period=0, skin_rel=0.0, warps=0):
+        check(self.lib.dpm2d_set_tuning(self.h, rebuild_period, skin_rel, warps))
+
+    def upload(self, xy):
+        xy = _f32(xy)
+        assert xy.size == 2 * self.nverts
+        check(self.lib.dpm2d_upload(self.h, xy.ctypes.data))
+
+    def upload_ptr(self, ptr: int):
+        check(self.lib.dpm2d_upload(self.h, ctypes.c_void_p(ptr)))
+
+    def step(self, nsteps: int, dt: float):
+        check(self.lib.dpm2d_step(self.h, nsteps, dt))
+
+    def download(self):
+        xy = np.empty((self.nverts, 2), np.float32)
+        F = np.empty((self.nverts, 2), np.float32)
+        check(self.lib.dpm2d_download(self.h, xy.ctypes.data, F.ctypes.data))
+        return xy, F
+
+    def download_ptr(self, xy_ptr: int, f_ptr: int = 0):
+        check(self.lib.dpm2d_download(self.h, ctypes.c_void_p(xy_ptr),
+                                      ctypes.c_void_p(f_ptr) if f_ptr else None))
+
+    def contained(self):
+        f = np.empty(self.nverts, np.uint8)
+        check(self.lib.dpm2d_last_contained(self.h, f.ctypes.data_as(_c_ubyte_p)))
+        return f
+
+    def areas(self):
+        a = np.empty(self.ncells, np.float32)
+        check(self.lib.dpm2d_cell_areas(self.h, fptr(a)))
+        return a
+
+    def stats(self):
+        r, f = ctypes.c_long(), ctypes.c_long()
+        check(self.lib.dpm2d_stats(self.h, ctypes.byref(r), ctypes.byref(f)))
+        return r.value, f.value
+
+    def step_kernel(self, dt: float):
+        check(self.lib.dpm2d_step_kernel(self.h, dt))
+
+    def rebuild_now(self):
+        check(self.lib.dpm2d_rebuild_now(self.h))
+
+    def cell_list(self):
+        n = self.ncells
+        keys = np.empty(n, np.uint32)
+        ids = np.empty(n, np.uint32)
+        nn = np.empty(n, np.int32)
+        maxnb = ctypes.c_int()
+        # first query the capacity
+        check(self.lib.dpm2d_cell_list(self.h, None, None, None, None, ctypes.byref(maxnb), None))
+        nbr = np.empty(n * maxnb.value, np.int32)
+        geom = np.empty((n, 8), np.float32)
+        check(self.lib.dpm2d_cell_list(self.h, keys.ctypes.data_as(_c_uint_p),
+                                       ids.ctypes.data_as(_c_uint_p),
+                                       nn.ctypes.data_as(_c_int_p), nbr.ctypes.data_as(_c_int_p),
+                                       ctypes.byref(maxnb), fptr(geom)))
+        return keys, ids, nn, nbr.reshape(n, maxnb.value), geom
+
+    def bins(self):
+        lb = ctypes.c_int()
+        nb = np.empty(self.ntissues, np.int32)
+        bw = np.empty(self.ntissues, np.float32)
+        sk = np.empty(self.ntissues, np.float32)
+        check(self.lib.dpm2d_bins(self.h, ctypes.byref(lb), nb.ctypes.data_as(_c_int_p), fptr(bw),
+                                  fptr(sk)))
+        return lb.value, nb, bw, sk
+
+    def close(self):
+        if self.h:
+            self.lib.dpm2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch3D:
+    """dpm3d_batch: independent 3D tissues sharing one mesh topology."""
+
+    def __init__(self, ctx: Context, ncells, faces, nv: int):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        nc = np.ascontiguousarray(ncells, dtype=np.int32)
+        f = np.ascontiguousarray(faces, dtype=np.uint32)
+        h = _vp()
+        check(self.lib.dpm3d_create(ctx.h, len(nc), nc.ctypes.data_as(_c_int_p), nv, len(f),
+                                    f.ctypes.data_as(_c_uint_p), ctypes.byref(h)))
+        self.h = h
+        self.ntissues = len(nc)
+        self.ncells = int(nc.sum())
+        self.nv = nv
+        self.nverts = self.ncells * nv
+
+    def set_cells(self, Kv, Ka, Ks, v0, a0, l0, Kb=None, adh=None):
+        arrs = [_f32(x) for x in (Kv, Ka, Ks, v0, a0, l0)]
+        kb = None if Kb is None else _f32(Kb)
+        ad = None if adh is None else _f32(adh)
+        check(self.lib.dpm3d_set_cells(self.h, *[fptr(x) for x in arrs],
+                                       None if kb is None else fptr(kb),
+                                       None if ad is None else fptr(ad)))
+
+    def set_tissues(self, L, Kre, pbc):
+        L, Kre = (_f32(np.broadcast_to(x, (self.ntissues,))) for x in (L, Kre))
+        p = np.ascontiguousarray(np.broadcast_to(pbc, (self.ntissues,)), dtype=np.int32)
+        check(self.lib.dpm3d_set_tissues(self.h, fptr(L), fptr(Kre), p.ctypes.data_as(_c_int_p)))
+
+    def set_tuning(self, rebuild_period=0, skin_rel=0.0):
+        check(self.lib.dpm3d_set_tuning(self.h, rebuild_period, skin_rel))
+
+    def upload(self, xyz):
+        xyz = _f32(xyz)
+        assert xyz.size == 3 * self.nverts
+        check(self.lib.dpm3d_upload(self.h, xyz.ctypes.data))
+
+    def step(self, nsteps: int, dt: float):
+        check(self.lib.dpm3d_step(self.h, nsteps, dt))
+
+    def download(self):
+        xyz = np.empty((self.nverts, 3), np.float32)
+        F = np.empty((self.nverts, 3), np.float32)
+        check(self.lib.dpm3d_download(self.h, xyz.ctypes.data, F.ctypes.data))
+        return xyz, F
+
+    def winding(self):
+        f = np.empty(self.nverts, np.uint8)
+        check(self.lib.dpm3d_last_winding(self.h, f.ctypes.data_as(_c_ubyte_p)))
+        return f
+
+    def close(self):
+        if self.h:
+            self.lib.dpm3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

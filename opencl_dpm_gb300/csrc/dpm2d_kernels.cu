@@ -1,0 +1,663 @@
+// 2D DPM kernels for sm_103a.
+//
+// One warp owns one cell per launch.  A time step is ONE fused kernel
+// (k2d_step): it reads the cell's vertex ring once, computes the area,
+// perimeter and bending forces from the ring held in shared memory, the
+// attraction and repulsion against the cells of its neighbour list, applies
+// the overdamped Euler update, writes the new positions, and -- as its
+// epilogue -- the geometry of the new positions (centre, enclosing radius,
+// area, box) that the next step's neighbour tests read.  The force field is
+// never stored unless the caller asks for the last step's forces.
+//
+// Physics follows the reference kernels (shaders/Cell2D_kernel.cl); the
+// repulsion's containment test uses the reference's exact crossing
+// arithmetic (each operation rounded separately, no contraction), so that a
+// vertex is flagged inside another cell on exactly the same inputs as the
+// reference flags it.  Candidate cells are pruned with tests that are proved
+// conservative (see `vertex_candidate`), so pruning never changes a flag.
+#include "dpm2d_kernels.cuh"
+
+#include <math.h>
+
+namespace dpm {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kRelMargin = 1e-5f;  // relative slack of the pruning tests
+constexpr float kAbsMargin = 1e-6f;  // per unit of coordinate magnitude
+
+// Geometry of the ring (sx, sy)[0..n) in shared memory: vertex mean, largest
+// distance to it, |shoelace area| (Cell2D_kernel.cl:25-36 form), box.
+__device__ Geom2D ring_geom(const float *sx, const float *sy, int n, int lane) {
+  float sumx = 0.f, sumy = 0.f, ar = 0.f;
+  float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+  for (int k = lane; k < n; k += 32) {
+    const float x = sx[k], y = sy[k];
+    const int km = k == 0 ? n - 1 : k - 1;
+    sumx += x;
+    sumy += y;
+    ar += 0.5f * ((sx[km] + x) * (sy[km] - y));
+    mnx = fminf(mnx, x);
+    mxx = fmaxf(mxx, x);
+    mny = fminf(mny, y);
+    mxy = fmaxf(mxy, y);
+  }
+  Geom2D g;
+  g.cx = warp_sum(sumx) / (float)n;
+  g.cy = warp_sum(sumy) / (float)n;
+  g.area = fabsf(warp_sum(ar));
+  g.minx = warp_min(mnx);
+  g.maxx = warp_max(mxx);
+  g.miny = warp_min(mny);
+  g.maxy = warp_max(mxy);
+  float r2 = 0.f;
+  for (int k = lane; k < n; k += 32) {
+    const float dx = sx[k] - g.cx, dy = sy[k] - g.cy;
+    r2 = fmaxf(r2, dx * dx + dy * dy);
+  }
+  g.R = sqrtf(warp_max(r2));
+  return g;
+}
+
+// One edge of the reference's crossing-number test (Cell2D_kernel.cl:171-195)
+// for the point (X, Y) and the edge (P_i, P_j), j = i-1: offsets d = v - P,
+// shifted per axis by L*floor (x) or L*round (y) when that edge has |d| > L,
+// then the half-open y test and the sign of the x intercept.  Every
+// operation is rounded on its own, as in the reference.
+__device__ __forceinline__ unsigned edge_crosses(float X, float Y, float pix, float piy,
+                                                 float pjx, float pjy, bool pbc, float L) {
+  float dix = __fsub_rn(X, pix), diy = __fsub_rn(Y, piy);
+  float djx = __fsub_rn(X, pjx), djy = __fsub_rn(Y, pjy);
+  if (pbc) {
+    if (fabsf(dix) > L || fabsf(djx) > L) {
+      dix = __fsub_rn(dix, __fmul_rn(L, floorf(__fdiv_rn(dix, L))));
+      djx = __fsub_rn(djx, __fmul_rn(L, floorf(__fdiv_rn(djx, L))));
+    }
+    if (fabsf(diy) > L || fabsf(djy) > L) {
+      diy = __fsub_rn(diy, __fmul_rn(L, roundf(__fdiv_rn(diy, L))));
+      djy = __fsub_rn(djy, __fmul_rn(L, roundf(__fdiv_rn(djy, L))));
+    }
+  }
+  if ((diy > 0.0f) == (djy > 0.0f)) return 0u;
+  const float r = __fadd_rn(
+      __fdiv_rn(__fmul_rn(__fsub_rn(djx, dix), __fsub_rn(0.0f, diy)), __fsub_rn(djy, diy)),
+      dix);
+  return 0.0f < r ? 1u : 0u;
+}
+
+// Can the reference's crossing test flag (X, Y) inside cell j?
+//  * If no edge of j is shifted (every |X - P.x| <= L and |Y - P.y| <= L),
+//    an odd count needs miny < Y <= maxy (the y test compares exact signs)
+//    and (X, Y) within the enclosing circle: outside it, (X, Y) is farther
+//    than the margin from every edge, so every x intercept has its true
+//    sign and the count equals the even-odd containment, which is 0.
+//  * A shift happens only if some vertex is more than L away on an axis;
+//    by monotone rounding that is decided exactly by the box corners.
+__device__ __forceinline__ bool vertex_candidate(float X, float Y, const Geom2D &gj,
+                                                 bool near, bool far, float L) {
+  if (near) {
+    const float dx = X - gj.cx, dy = Y - gj.cy;
+    const float rm = gj.R * (1.0f + kRelMargin) +
+                     kAbsMargin * (fabsf(gj.cx) + fabsf(gj.cy) + fabsf(X) + fabsf(Y));
+    const float bm = kRelMargin * (gj.maxx - gj.minx) +
+                     kAbsMargin * (fabsf(gj.minx) + fabsf(gj.maxx) + fabsf(X));
+    if (Y > gj.miny && Y <= gj.maxy && X >= gj.minx - bm && X <= gj.maxx + bm &&
+        dx * dx + dy * dy <= rm * rm)
+      return true;
+  }
+  if (far) {
+    if (__fsub_rn(X, gj.minx) > L || __fsub_rn(gj.maxx, X) > L ||
+        __fsub_rn(Y, gj.miny) > L || __fsub_rn(gj.maxy, Y) > L)
+      return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void normalize2(float x, float y, float &ox, float &oy) {
+  const float l2 = x * x + y * y;
+  if (l2 == 0.0f) {
+    ox = x;
+    oy = y;
+    return;
+  }
+  const float l = sqrtf(l2);
+  ox = x / l;
+  oy = y / l;
+}
+
+// ---------------------------------------------------------------------------
+// Initial geometry
+// ---------------------------------------------------------------------------
+
+constexpr int kGeomWarps = 8;
+
+__global__ void __launch_bounds__(kGeomWarps * 32)
+    k2d_geom(const Cell2D *__restrict__ cells, const float2 *__restrict__ pos,
+             Geom2D *__restrict__ geom, int ncells) {
+  __shared__ float shx[kGeomWarps][kMaxNV2D], shy[kGeomWarps][kMaxNV2D];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kGeomWarps + w;
+  if (c >= ncells) return;
+  const Cell2D cp = cells[c];
+  const int n = (int)cp.nv;
+  for (int k = lane; k < n; k += 32) {
+    const float2 v = pos[cp.voff + k];
+    shx[w][k] = v.x;
+    shy[w][k] = v.y;
+  }
+  __syncwarp();
+  const Geom2D g = ring_geom(shx[w], shy[w], n, lane);
+  if (lane == 0) geom[c] = g;
+}
+
+// ---------------------------------------------------------------------------
+// Cell list: per-tissue bins and keys
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int bin_count_dev(float L, float w, int cap) {
+  int nb = (int)floorf(__fdiv_rn(L, w));
+  return max(1, min(nb, cap));
+}
+
+__device__ __forceinline__ int bin_of(float x, float L, float inv, int nb) {
+  int b = (int)floorf(__fmul_rn(wrap_rn(x, L), inv));
+  return max(0, min(b, nb - 1));
+}
+
+__device__ __forceinline__ float block_reduce_max(float v, float *sh) {
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  float r = -INFINITY;
+  for (int i = 0; i < nw; ++i) r = fmaxf(r, sh[i]);
+  return r;
+}
+__device__ __forceinline__ float block_reduce_min(float v, float *sh) {
+  return -block_reduce_max(-v, sh);
+}
+
+__global__ void __launch_bounds__(256) k2d_binprep(Rebuild2DArgs a, int local_bits) {
+  __shared__ float red[32];
+  const int t = blockIdx.x;
+  const Tissue2D T = a.tissues[t];
+  float dmax = 0.f, mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+  for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x) {
+    const Geom2D g = a.geom[c];
+    dmax = fmaxf(dmax, 2.0f * g.R);
+    mnx = fminf(mnx, g.minx);
+    mxx = fmaxf(mxx, g.maxx);
+    mny = fminf(mny, g.miny);
+    mxy = fmaxf(mxy, g.maxy);
+  }
+  dmax = block_reduce_max(dmax, red);
+  mnx = block_reduce_min(mnx, red);
+  mxx = block_reduce_max(mxx, red);
+  mny = block_reduce_min(mny, red);
+  mxy = block_reduce_max(mxy, red);
+  float w = __fadd_rn(dmax, T.skin);
+  w = __fadd_rn(w, __fadd_rn(__fmul_rn(1e-3f, dmax), __fmul_rn(1e-5f, T.L)));
+  if (T.Kat != 0.0f) w = __fadd_rn(w, T.l0max);
+  const int nb = bin_count_dev(T.L, w, T.cap);
+  if (threadIdx.x == 0) {
+    Tissue2D *o = a.tissues + t;
+    o->binw = w;
+    o->nbx = nb;
+    o->nby = nb;
+    o->gminx = mnx;
+    o->gmaxx = mxx;
+    o->gminy = mny;
+    o->gmaxy = mxy;
+    a.stale[t] = 0;
+  }
+  const float inv = __fdiv_rn((float)nb, T.L);
+  for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x) {
+    const Geom2D g = a.geom[c];
+    const int bx = bin_of(g.cx, T.L, inv, nb), by = bin_of(g.cy, T.L, inv, nb);
+    a.keys[c] = ((uint32_t)t << local_bits) | (uint32_t)(by * nb + bx);
+    a.vals[c] = (uint32_t)c;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cell list: neighbour lists
+// ---------------------------------------------------------------------------
+
+constexpr int kNbWarps = 8;
+constexpr int kNbBuf = 128;
+static_assert(kNbBuf >= kMaxNB2D + 32, "neighbour buffer too small");
+
+__device__ __forceinline__ int lower_bound_u32(const uint32_t *a, int lo, int hi, uint32_t key) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Does pair (i, j) need to be in i's list for the next rebuild period?
+// Distances may change by at most the skin before the list is rebuilt or
+// declared stale (each cell's box and circle move by at most skin/2).
+// The rebuild tests below use separately rounded operations only, in a fixed
+// order, so that a host rebuild with IEEE float32 arithmetic reproduces the
+// neighbour lists bit for bit.
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+
+// Slack of the rebuild tests: well above the per-step tests' margins.
+__device__ __forceinline__ float rebuild_margin(const Geom2D &gi, const Geom2D &gj,
+                                                const Tissue2D &T) {
+  const float mag =
+      fa(fa(fa(fa(fabsf(gi.cx), fabsf(gi.cy)), fabsf(gj.cx)), fabsf(gj.cy)), T.L);
+  return fa(fm(1e-3f, fa(gi.R, gj.R)), fm(1e-4f, mag));
+}
+
+__device__ __forceinline__ float round_away(float x) { return roundf(x); }
+
+__device__ __forceinline__ bool pair_near(const Geom2D &gi, const Geom2D &gj,
+                                          const Tissue2D &T, float l0) {
+  const float dx = fs(gi.cx, gj.cx), dy = fs(gi.cy, gj.cy);
+  const float m = rebuild_margin(gi, gj, T);
+  const float r = fa(fa(fa(gi.R, gj.R), T.skin), m);
+  if (fa(fm(dx, dx), fm(dy, dy)) <= fm(r, r)) return true;
+  if (T.Kat != 0.0f) {
+    float ex = dx, ey = dy;
+    if (T.pbc) {
+      ex = fs(ex, fm(T.L, round_away(__fdiv_rn(ex, T.L))));
+      ey = fs(ey, fm(T.L, round_away(__fdiv_rn(ey, T.L))));
+    }
+    const float ra = fa(r, fmaxf(l0, T.l0max));
+    if (fa(fm(ex, ex), fm(ey, ey)) <= fm(ra, ra)) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool pair_far(const Geom2D &gi, const Geom2D &gj, const Tissue2D &T) {
+  if (!T.pbc) return false;
+  const float lim = fs(fs(T.L, T.skin), rebuild_margin(gi, gj, T));
+  return fs(gi.maxx, gj.minx) >= lim || fs(gj.maxx, gi.minx) >= lim ||
+         fs(gi.maxy, gj.miny) >= lim || fs(gj.maxy, gi.miny) >= lim;
+}
+
+__device__ __forceinline__ bool cell_on_boundary(const Geom2D &gi, const Tissue2D &T) {
+  if (!T.pbc) return false;
+  // any far partner j passes the pair test against the tissue extent, with
+  // a margin at least as large as rebuild_margin(gi, gj)
+  const float ext = fa(fa(fa(fabsf(T.gminx), fabsf(T.gmaxx)), fabsf(T.gminy)), fabsf(T.gmaxy));
+  const float own = fa(fa(fabsf(gi.cx), fabsf(gi.cy)), T.L);
+  const float m = fa(fa(fm(2e-3f, fa(gi.R, T.binw)), fm(1e-4f, own)), fm(2e-4f, ext));
+  const float lim = fs(fs(T.L, T.skin), m);
+  return fs(gi.maxx, T.gminx) >= lim || fs(T.gmaxx, gi.minx) >= lim ||
+         fs(gi.maxy, T.gminy) >= lim || fs(T.gmaxy, gi.miny) >= lim;
+}
+
+__global__ void __launch_bounds__(kNbWarps * 32) k2d_neighbors(Rebuild2DArgs a, int local_bits) {
+  __shared__ int buf[kNbWarps][kNbBuf];
+  __shared__ unsigned char uniq[kNbWarps][kNbBuf];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kNbWarps + w;
+  if (c >= a.ncells) return;
+  const Cell2D cp = a.cells[c];
+  const int t = (int)cp.tissue;
+  const Tissue2D T = a.tissues[t];
+  const Geom2D gi = a.geom[c];
+  const unsigned lt = (1u << lane) - 1u;
+  int cnt = 0;
+
+  const int nb = T.nbx;
+  const float inv = __fdiv_rn((float)nb, T.L);
+  const int bx = bin_of(gi.cx, T.L, inv, nb), by = bin_of(gi.cy, T.L, inv, nb);
+  // distinct bin offsets along an axis with nb bins
+  const int lo_off = nb >= 3 ? -1 : 0, hi_off = nb >= 3 ? 1 : nb - 1;
+  for (int oy = lo_off; oy <= hi_off; ++oy) {
+    const int yy = (by + oy + nb) % nb;
+    for (int ox = lo_off; ox <= hi_off; ++ox) {
+      const int xx = (bx + ox + nb) % nb;
+      const uint32_t key = ((uint32_t)t << local_bits) | (uint32_t)(yy * nb + xx);
+      const int lo = lower_bound_u32(a.sorted_keys, T.cell_begin, T.cell_end, key);
+      const int hi = lower_bound_u32(a.sorted_keys, lo, T.cell_end, key + 1u);
+      for (int base = lo; base < hi; base += 32) {
+        const int q = base + lane;
+        const int j = q < hi ? (int)a.sorted_vals[q] : -1;
+        const bool ok = j >= 0 && j != c && pair_near(gi, a.geom[j], T, cp.l0);
+        const unsigned m = __ballot_sync(kFull, ok);
+        const int pos = cnt + __popc(m & lt);
+        if (ok && pos < kNbBuf) buf[w][pos] = j;
+        cnt += __popc(m);
+      }
+    }
+  }
+  // pairs whose raw offsets can exceed L (the reference's shifted edges)
+  if (cell_on_boundary(gi, T)) {
+    for (int base = T.cell_begin; base < T.cell_end; base += 32) {
+      const int j = base + lane;
+      const bool ok = j < T.cell_end && j != c && pair_far(gi, a.geom[j], T);
+      const unsigned m = __ballot_sync(kFull, ok);
+      const int pos = cnt + __popc(m & lt);
+      if (ok && pos < kNbBuf) buf[w][pos] = j;
+      cnt += __popc(m);
+    }
+  }
+  __syncwarp();
+  int nout;
+  if (cnt > kNbBuf) {
+    nout = kNbOverflow;
+  } else {
+    // drop duplicates, then place each unique id at its rank (ascending ids)
+    for (int i = lane; i < cnt; i += 32) {
+      const int v = buf[w][i];
+      bool first = true;
+      for (int k = 0; k < i; ++k) first &= buf[w][k] != v;
+      uniq[w][i] = first ? 1 : 0;
+    }
+    __syncwarp();
+    int nu = 0;
+    for (int i = 0; i < cnt; ++i) nu += uniq[w][i];
+    if (nu > kMaxNB2D) {
+      nout = kNbOverflow;
+    } else {
+      int *out = a.nbr + (size_t)c * kMaxNB2D;
+      for (int i = lane; i < cnt; i += 32) {
+        if (!uniq[w][i]) continue;
+        const int v = buf[w][i];
+        int rank = 0;
+        for (int k = 0; k < cnt; ++k) rank += (uniq[w][k] && buf[w][k] < v) ? 1 : 0;
+        out[rank] = v;
+      }
+      nout = nu;
+    }
+  }
+  if (lane == 0) {
+    a.nn[c] = nout;
+    a.geom0[c] = gi;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused step
+// ---------------------------------------------------------------------------
+
+template <int S, int W>
+__global__ void __launch_bounds__(W * 32) k2d_step(Step2DArgs a) {
+  constexpr int M = 32 * S;
+  __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
+  __shared__ unsigned char sh_f[W][M];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * W + w;
+  if (c >= a.ncells) return;
+  float *sx = sh_x[w], *sy = sh_y[w], *nxs = sh_nx[w], *nys = sh_ny[w];
+  unsigned char *sf = sh_f[w];
+
+  const Cell2D cp = a.cells[c];
+  const int tid = (int)cp.tissue;
+  const Tissue2D T = a.tissues[tid];
+  const int n = (int)cp.nv;
+  const float L = T.L;
+  const bool pbc = T.pbc != 0;
+
+  float vx[S], vy[S], fx[S], fy[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const int k = lane + 32 * s;
+    vx[s] = vy[s] = fx[s] = fy[s] = 0.0f;
+    if (k < n) {
+      const float2 v = a.pos_in[cp.voff + k];
+      vx[s] = v.x;
+      vy[s] = v.y;
+      sx[k] = v.x;
+      sy[k] = v.y;
+      sf[k] = 0;
+    }
+  }
+  __syncwarp();
+  const Geom2D gi = a.geom_in[c];
+
+  // -- shape forces: area (AreaForceUpdates, with the reference's sign of
+  // the y term), perimeter (PerimeterForceUpdates), bending
+  // (BendingForceUpdates); summed in the reference's order.
+  const float strain = gi.area / cp.a0 - 1.0f;
+  const float ka = cp.kA * 0.5f * strain;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const int k = lane + 32 * s;
+    if (k < n) {
+      const int im1 = k == 0 ? n - 1 : k - 1;
+      const int ip1 = k == n - 1 ? 0 : k + 1;
+      const int im2 = im1 == 0 ? n - 1 : im1 - 1;
+      const int ip2 = ip1 == n - 1 ? 0 : ip1 + 1;
+      const float x = vx[s], y = vy[s];
+      const float xm = sx[im1], ym = sy[im1], xp = sx[ip1], yp = sy[ip1];
+      const float xmm = sx[im2], ymm = sy[im2], xpp = sx[ip2], ypp = sy[ip2];
+      const float ax = ka * (ym - yp), ay = ka * (xm - xp);
+      const float lvx = xp - x, lvy = yp - y, lmx = x - xm, lmy = y - ym;
+      const float len = sqrtf(lvx * lvx + lvy * lvy), lenm = sqrtf(lmx * lmx + lmy * lmy);
+      const float dl = len / cp.l0 - 1.0f, dlm = lenm / cp.l0 - 1.0f;
+      const float px = cp.kL * (dl * (lvx / len) - dlm * (lmx / lenm));
+      const float py = cp.kL * (dl * (lvy / len) - dlm * (lmy / lenm));
+      const float six = lvx - lmx, siy = lvy - lmy;
+      const float sixp = (xpp - xp) - lvx, siyp = (ypp - yp) - lvy;
+      const float sixm = lmx - (xm - xmm), siym = lmy - (ym - ymm);
+      const float bx = cp.Kb * (2.0f * six - sixm - sixp);
+      const float by = cp.Kb * (2.0f * siy - siym - siyp);
+      fx[s] = (ax + px) + bx;
+      fy[s] = (ay + py) + by;
+    }
+  }
+
+  // -- attraction and repulsion against the neighbour list (cells in
+  // ascending order, as the reference loops over them).
+  const int nnc = a.nn[c];
+  const bool scan_all =
+      nnc == kNbOverflow || *((volatile const int *)(a.stale + tid)) != 0;
+  const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
+  const int *list = a.nbr + (size_t)c * kMaxNB2D;
+  const bool att = T.Kat != 0.0f;
+  for (int q = 0; q < count; ++q) {
+    const int j = scan_all ? T.cell_begin + q : list[q];
+    if (j == c) continue;
+    const Geom2D gj = a.geom_in[j];
+    const float dcx = gi.cx - gj.cx, dcy = gi.cy - gj.cy;
+    const float rr = gi.R + gj.R;
+    const float mm = kRelMargin * rr +
+                     kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) + fabsf(gj.cx) + fabsf(gj.cy));
+    const bool near = dcx * dcx + dcy * dcy <= (rr + mm) * (rr + mm);
+    const bool far = pbc && (__fsub_rn(gi.maxx, gj.minx) > L || __fsub_rn(gj.maxx, gi.minx) > L ||
+                             __fsub_rn(gi.maxy, gj.miny) > L || __fsub_rn(gj.maxy, gi.miny) > L);
+    bool attp = false;
+    if (att) {
+      float ex = dcx, ey = dcy;
+      if (pbc) {
+        ex -= L * roundf(ex / L);
+        ey -= L * roundf(ey / L);
+      }
+      const float ra = rr + cp.l0 + mm;
+      attp = ex * ex + ey * ey <= ra * ra;
+    }
+    if (!near && !far && !attp) continue;
+
+    unsigned cm[S], am[S];
+    bool anyc = false, anya = false;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int k = lane + 32 * s;
+      bool cand = false, ac = false;
+      if (k < n) {
+        if (!sf[k]) cand = vertex_candidate(vx[s], vy[s], gj, near, far, L);
+        if (attp) {
+          float ex = gj.cx - vx[s], ey = gj.cy - vy[s];
+          if (pbc) {
+            ex -= L * roundf(ex / L);
+            ey -= L * roundf(ey / L);
+          }
+          const float ra = gj.R + cp.l0 + mm;
+          ac = ex * ex + ey * ey <= ra * ra;
+        }
+      }
+      cm[s] = __ballot_sync(kFull, cand);
+      am[s] = __ballot_sync(kFull, ac);
+      anyc |= cm[s] != 0u;
+      anya |= am[s] != 0u;
+    }
+    if (!anyc && !anya) continue;
+
+    // stage the neighbour's ring
+    const uint4 jr = *reinterpret_cast<const uint4 *>(a.cells + j);
+    const int nj = (int)jr.y;
+    const float2 *pj = a.pos_in + jr.x;
+    for (int k = lane; k < nj; k += 32) {
+      const float2 v = pj[k];
+      nxs[k] = v.x;
+      nys[k] = v.y;
+    }
+    __syncwarp();
+
+    if (anya) {
+      // AttractionForceUpdate (Cell2D_kernel.cl:251-267)
+      const float kat = T.Kat / (float)n;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        if (!((am[s] >> lane) & 1u)) continue;
+        for (int v = 0; v < nj; ++v) {
+          float rx = nxs[v] - vx[s], ry = nys[v] - vy[s];
+          if (pbc) {
+            rx -= L * roundf(rx / L);
+            ry -= L * roundf(ry / L);
+          }
+          const float dist = sqrtf(rx * rx + ry * ry);
+          if (dist < cp.l0) {
+            const float ftmp = kat * dist / cp.l0;
+            float ux, uy;
+            normalize2(rx, ry, ux, uy);
+            fx[s] += ftmp * ux;
+            fy[s] += ftmp * uy;
+          }
+        }
+      }
+    }
+    if (anyc) {
+      // RepulsionForceUpdate containment (Cell2D_kernel.cl:166-202):
+      // lanes take the edges, a ballot gives the crossing parity.
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        unsigned msk = cm[s];
+        while (msk) {
+          const int l = __ffs(msk) - 1;
+          msk &= msk - 1u;
+          const int v = l + 32 * s;
+          const float X = sx[v], Y = sy[v];
+          unsigned par = 0u;
+          for (int e = lane; e < nj; e += 32) {
+            const int ep = e == 0 ? nj - 1 : e - 1;
+            par ^= edge_crosses(X, Y, nxs[e], nys[e], nxs[ep], nys[ep], pbc, L);
+          }
+          const unsigned bal = __ballot_sync(kFull, par != 0u);
+          if ((__popc(bal) & 1) && lane == 0) sf[v] = 1;
+        }
+      }
+    }
+    __syncwarp();
+  }
+
+  // -- repulsion force toward the own centre (Cell2D_kernel.cl:205-219)
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const int k = lane + 32 * s;
+    if (k < n && sf[k]) {
+      float dx = gi.cx - vx[s], dy = gi.cy - vy[s];
+      if (pbc) {
+        dx -= L * roundf(dx / L);
+        dy -= L * roundf(dy / L);
+      }
+      const float dist = sqrtf(dx * dx + dy * dy);
+      const float xij = dist / (2.0f * cp.r0);
+      const float ftmp = T.Kre * (1.0f - xij);
+      float ux, uy;
+      normalize2(dx, dy, ux, uy);
+      fx[s] += 0.5f * ftmp * ux;
+      fy[s] += 0.5f * ftmp * uy;
+    }
+  }
+
+  // -- Euler update (EulerUpdate, Cell2D_kernel.cl:279) and outputs
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const int k = lane + 32 * s;
+    if (k < n) {
+      const float nxv = __fadd_rn(vx[s], __fmul_rn(fx[s], a.dt));
+      const float nyv = __fadd_rn(vy[s], __fmul_rn(fy[s], a.dt));
+      a.pos_out[cp.voff + k] = make_float2(nxv, nyv);
+      if (a.force_out) a.force_out[cp.voff + k] = make_float2(fx[s], fy[s]);
+      if (a.flags_out) a.flags_out[cp.voff + k] = sf[k];
+      sx[k] = nxv;
+      sy[k] = nyv;
+    }
+  }
+  __syncwarp();
+
+  // -- epilogue: geometry of the new positions for the next step
+  const Geom2D g = ring_geom(sx, sy, n, lane);
+  if (lane == 0) {
+    a.geom_out[c] = g;
+    if (!(isfinite(g.cx) && isfinite(g.cy) && isfinite(g.R))) atomicOr(a.err, 1);
+    const Geom2D g0 = a.geom0[c];
+    const float dc = sqrtf((g.cx - g0.cx) * (g.cx - g0.cx) + (g.cy - g0.cy) * (g.cy - g0.cy));
+    float d = dc + fmaxf(0.0f, g.R - g0.R);
+    d = fmaxf(d, fmaxf(fabsf(g.minx - g0.minx), fabsf(g.maxx - g0.maxx)));
+    d = fmaxf(d, fmaxf(fabsf(g.miny - g0.miny), fabsf(g.maxy - g0.maxy)));
+    if (!(d <= 0.5f * T.skin)) atomicOr(a.stale + tid, 1);
+  }
+}
+
+template <int S, int W>
+cudaError_t launch_step_sw(const Step2DArgs &a, cudaStream_t s) {
+  const int grid = (a.ncells + W - 1) / W;
+  k2d_step<S, W><<<grid, W * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int S>
+cudaError_t launch_step_s(const Step2DArgs &a, int warps, cudaStream_t s) {
+  // 16 warps of 8 slots would exceed the static shared-memory limit
+  if (warps == 4) return launch_step_sw<S, 4>(a, s);
+  if (warps == 16 && S <= 4) return launch_step_sw<S, (S <= 4 ? 16 : 8)>(a, s);
+  return launch_step_sw<S, 8>(a, s);
+}
+
+} // namespace
+
+int bin_axis_count(float L, float w, int cap) {
+  int nb = (int)floorf(L / w);
+  return nb < 1 ? 1 : (nb > cap ? cap : nb);
+}
+
+cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom, int ncells,
+                          int maxnv, cudaStream_t s) {
+  (void)maxnv;
+  const int grid = (ncells + kGeomWarps - 1) / kGeomWarps;
+  k2d_geom<<<grid, kGeomWarps * 32, 0, s>>>(cells, pos, geom, ncells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s) {
+  k2d_binprep<<<a.ntissues, 256, 0, s>>>(a, local_bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s) {
+  const int grid = (a.ncells + kNbWarps - 1) / kNbWarps;
+  k2d_neighbors<<<grid, kNbWarps * 32, 0, s>>>(a, local_bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, cudaStream_t s) {
+  if (maxnv <= 32) return launch_step_s<1>(a, warps, s);
+  if (maxnv <= 64) return launch_step_s<2>(a, warps, s);
+  if (maxnv <= 128) return launch_step_s<4>(a, warps, s);
+  return launch_step_s<8>(a, warps, s);
+}
+
+} // namespace dpm

@@ -1,0 +1,56 @@
+// 2D DPM kernels: launch interface.
+#pragma once
+
+#include "dpm_common.cuh"
+
+namespace dpm {
+
+struct Step2DArgs {
+  const Cell2D *cells;
+  const Tissue2D *tissues;
+  const float2 *pos_in;
+  float2 *pos_out;
+  float2 *force_out;        // forces of this step, or nullptr
+  unsigned char *flags_out; // containment flags of this step, or nullptr
+  const Geom2D *geom_in;    // geometry of pos_in
+  Geom2D *geom_out;         // geometry of pos_out (written)
+  const Geom2D *geom0;      // geometry at the last neighbour-list rebuild
+  const int *nn;            // neighbour counts (kNbOverflow = scan tissue)
+  const int *nbr;           // neighbour lists, kMaxNB2D per cell
+  int *stale;               // per tissue: list no longer covers all pairs
+  int *err;                 // bit 0: non-finite positions
+  int ncells;
+  float dt;
+};
+
+struct Rebuild2DArgs {
+  const Cell2D *cells;
+  Tissue2D *tissues;
+  const Geom2D *geom;
+  Geom2D *geom0;
+  uint32_t *keys;
+  uint32_t *vals;
+  const uint32_t *sorted_keys;
+  const uint32_t *sorted_vals;
+  int *nn;
+  int *nbr;
+  int *stale;
+  int ncells;
+  int ntissues;
+};
+
+// Geometry of every cell (circle, area, box) from positions.
+cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom,
+                          int ncells, int maxnv, cudaStream_t s);
+// Per-tissue bin sizes and per-cell bin keys (one block per tissue).
+cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
+// Neighbour lists from the sorted cell list (one warp per cell).
+cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
+// One fused time step.
+cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps,
+                          cudaStream_t s);
+
+// Host mirror of the bin arithmetic (for the host rebuild check).
+int bin_axis_count(float L, float w, int cap);
+
+} // namespace dpm

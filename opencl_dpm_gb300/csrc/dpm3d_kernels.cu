@@ -1,0 +1,576 @@
+// 3D DPM kernels for sm_103a.
+//
+// One thread block owns one cell per step and keeps the cell's mesh in
+// shared memory.  A step is one fused kernel (k3d_step):
+//   * centre of mass (from the previous step's epilogue) and volume (block
+//     reduction over faces);
+//   * volume, surface-area and substrate forces per vertex, gathered over
+//     the vertex's incident faces in ascending face order -- the order in
+//     which the reference's compare-and-swap adds reach a vertex when its
+//     work-items run in order -- so no atomics are needed and the result is
+//     deterministic (shaders/Cell3D_Kernel.cl:66-247);
+//   * optional triangle bending (extension);
+//   * repulsion by winding number against the cells of the neighbour list
+//     (Cell3D_Kernel.cl:251-310): candidate vertices inside the neighbour's
+//     bounding sphere are compacted, one warp evaluates one candidate's
+//     solid-angle sum over the neighbour's faces with the neighbour's
+//     vertices staged in shared memory;
+//   * Euler update x += F*dt (Cell3D_Kernel.cl:371-381) and, as epilogue, the
+//     centre and bounding radius of the new mesh for the next step.
+#include "dpm3d_kernels.cuh"
+
+#include <math.h>
+
+namespace dpm {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct f3 {
+  float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// normalize with the OpenCL special case: the zero vector maps to itself
+__device__ __forceinline__ f3 normalize(f3 a) {
+  const float l2 = dot(a, a);
+  if (l2 == 0.0f) return a;
+  return a / sqrtf(l2);
+}
+
+__device__ float block_sum(float v, float *red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  float r = 0.0f;
+  for (int i = 0; i < kWarps; ++i) r += red[i];
+  return r;
+}
+__device__ float block_max(float v, float *red) {
+  v = warp_max(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  float r = -INFINITY;
+  for (int i = 0; i < kWarps; ++i) r = fmaxf(r, red[i]);
+  return r;
+}
+
+// Centre of mass (sum times 1/NV, Cell3D_Kernel.cl:35-44) and bounding
+// radius of the mesh held in shared memory.
+__device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, int nv,
+                            float *red) {
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  for (int v = threadIdx.x; v < nv; v += kThreads) {
+    sx += px[v];
+    sy += py[v];
+    sz += pz[v];
+  }
+  const float inv = 1.0f / (float)nv;
+  Geom3D g;
+  g.cx = block_sum(sx, red) * inv;
+  g.cy = block_sum(sy, red) * inv;
+  g.cz = block_sum(sz, red) * inv;
+  float r2 = 0.f;
+  for (int v = threadIdx.x; v < nv; v += kThreads) {
+    const float dx = px[v] - g.cx, dy = py[v] - g.cy, dz = pz[v] - g.cz;
+    r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+  }
+  g.R = sqrtf(block_max(r2, red));
+  return g;
+}
+
+// Shared-memory layout of k3d_step (see step3d_smem_bytes).
+struct Smem3D {
+  float *px, *py, *pz, *fx, *fy, *fz, *qx, *qy, *qz, *ux, *uy, *uz, *red;
+  float *bnx, *bny, *bnz, *bnl, *bgx, *bgy, *bgz;
+  int *ncand;
+  uint16_t *faces, *cand;
+  unsigned char *wnc;
+};
+
+__device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
+  Smem3D s;
+  float *f = reinterpret_cast<float *>(base);
+  s.px = f; f += nv;
+  s.py = f; f += nv;
+  s.pz = f; f += nv;
+  s.fx = f; f += nv;
+  s.fy = f; f += nv;
+  s.fz = f; f += nv;
+  s.qx = f; f += nv;
+  s.qy = f; f += nv;
+  s.qz = f; f += nv;
+  s.ux = f; f += kWarps * nv;
+  s.uy = f; f += kWarps * nv;
+  s.uz = f; f += kWarps * nv;
+  s.red = f; f += 64;
+  if (bend) {
+    s.bnx = f; f += nf;
+    s.bny = f; f += nf;
+    s.bnz = f; f += nf;
+    s.bnl = f; f += nf;
+    s.bgx = f; f += nf;
+    s.bgy = f; f += nf;
+    s.bgz = f; f += nf;
+  } else {
+    s.bnx = s.bny = s.bnz = s.bnl = s.bgx = s.bgy = s.bgz = nullptr;
+  }
+  s.ncand = reinterpret_cast<int *>(f);
+  f += 4;
+  uint16_t *h = reinterpret_cast<uint16_t *>(f);
+  s.faces = h;
+  h += 3 * nf;
+  s.cand = h;
+  h += nv;
+  s.wnc = reinterpret_cast<unsigned char *>(h);
+  return s;
+}
+
+__device__ __forceinline__ f3 vtx(const Smem3D &s, int i) { return mk(s.px[i], s.py[i], s.pz[i]); }
+
+__global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
+  extern __shared__ __align__(16) char smem3d[];
+  const int c = blockIdx.x;
+  const int NV = a.mesh.nv, NF = a.mesh.nf;
+  const bool bend_any = a.bend != 0;
+  Smem3D s = carve(smem3d, NV, NF, bend_any);
+  const Cell3D P = a.cells[c];
+  const Tissue3D T = a.tissues[P.tissue];
+  const size_t base = (size_t)c * NV;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+
+  for (int v = tid; v < NV; v += kThreads) {
+    s.px[v] = a.xin[base + v];
+    s.py[v] = a.yin[base + v];
+    s.pz[v] = a.zin[base + v];
+    s.wnc[v] = 0;
+  }
+  for (int i = tid; i < 3 * NF; i += kThreads) s.faces[i] = a.mesh.faces[i];
+  __syncthreads();
+
+  const Geom3D gi = a.geom_in[c];
+  const f3 C = mk(gi.cx, gi.cy, gi.cz);
+
+  // volume (getVolume, Cell3D_Kernel.cl:46-64)
+  float vpart = 0.0f;
+  for (int f = tid; f < NF; f += kThreads) {
+    const f3 P0 = vtx(s, s.faces[3 * f]), P1 = vtx(s, s.faces[3 * f + 1]),
+             P2 = vtx(s, s.faces[3 * f + 2]);
+    vpart += dot(cross(P0, P1), P2) / 6.0f;
+  }
+  const float volume = fabsf(block_sum(vpart, s.red));
+  const float kvol = -P.Kv * (volume / P.v0 - 1.0f);
+
+  // triangle bending, face pass (extension): unit normals, then G per face
+  const bool bend = bend_any && P.Kb != 0.0f;
+  if (bend) {
+    for (int f = tid; f < NF; f += kThreads) {
+      const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
+               p2 = vtx(s, s.faces[3 * f + 2]);
+      const f3 n = cross(p1 - p0, p2 - p0);
+      const float l = sqrtf(dot(n, n));
+      const f3 nh = l > 0.0f ? n / l : mk(0.f, 0.f, 0.f);
+      s.bnx[f] = nh.x;
+      s.bny[f] = nh.y;
+      s.bnz[f] = nh.z;
+      s.bnl[f] = l;
+    }
+    __syncthreads();
+    for (int f = tid; f < NF; f += kThreads) {
+      f3 G = mk(0.f, 0.f, 0.f);
+      const float l = s.bnl[f];
+      if (l != 0.0f) {
+        const f3 nf = mk(s.bnx[f], s.bny[f], s.bnz[f]);
+        for (int e = 0; e < 3; ++e) {
+          const int g = a.mesh.adj[3 * f + e];
+          if (g < 0) continue;
+          const f3 ng = mk(s.bnx[g], s.bny[g], s.bnz[g]);
+          const float cth = dot(nf, ng);
+          G = G + (ng - cth * nf) / l;
+        }
+      }
+      s.bgx[f] = G.x;
+      s.bgy[f] = G.y;
+      s.bgz[f] = G.z;
+    }
+    __syncthreads();
+  }
+
+  // per-vertex shape forces, in the reference's accumulation order
+  const float range = P.adh;
+  for (int v = tid; v < NV; v += kThreads) {
+    f3 F = mk(0.f, 0.f, 0.f);
+    const int e0 = a.mesh.inc_off[v], e1 = a.mesh.inc_off[v + 1];
+    // VolumeForceUpdate (Cell3D_Kernel.cl:95-111)
+    if (P.Kv != 0.0f) {
+      for (int e = e0; e < e1; ++e) {
+        const int f = a.mesh.inc_face[e], k = a.mesh.inc_corner[e];
+        const f3 A = vtx(s, s.faces[3 * f + 1]) - C, B = vtx(s, s.faces[3 * f + 2]) - C,
+                 Cc = vtx(s, s.faces[3 * f]) - C;
+        const f3 g = k == 0 ? cross(A, B) : (k == 1 ? cross(B, Cc) : cross(Cc, A));
+        F = F + (kvol * g) / 6.0f;
+      }
+    }
+    // SurfaceAreaForceUpdate (Cell3D_Kernel.cl:129-176)
+    if (!(P.Ka < 1e-8f)) {
+      for (int e = e0; e < e1; ++e) {
+        const int f = a.mesh.inc_face[e], k = a.mesh.inc_corner[e];
+        const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
+                 p2 = vtx(s, s.faces[3 * f + 2]);
+        const f3 lv0 = p1 - p0, lv1 = p2 - p1, lv2 = p0 - p2;
+        const float L0 = sqrtf(dot(lv0, lv0)), L1 = sqrtf(dot(lv1, lv1)),
+                    L2 = sqrtf(dot(lv2, lv2));
+        if (L0 < 1e-12f || L1 < 1e-12f || L2 < 1e-12f) continue;
+        const f3 n0 = lv0 / L0, n1 = lv1 / L1, n2 = lv2 / L2;
+        const float d0 = L0 / P.l0 - 1.0f, d1 = L1 / P.l0 - 1.0f, d2 = L2 / P.l0 - 1.0f;
+        f3 g;
+        if (k == 0) g = d0 * n0 - d2 * n2;
+        else if (k == 1) g = d1 * n1 - d0 * n0;
+        else g = d2 * n2 - d1 * n1;
+        F = F + P.sa_scale * g;
+      }
+    }
+    // StickToSurface (Cell3D_Kernel.cl:196-246)
+    if (!(P.Ks < 1e-12f)) {
+      for (int e = e0; e < e1; ++e) {
+        const int f = a.mesh.inc_face[e], k = a.mesh.inc_corner[e];
+        const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
+                 p2 = vtx(s, s.faces[3 * f + 2]);
+        const f3 un = normalize(cross(p1 - p0, p2 - p0));
+        if (!(un.z < -0.1f)) continue;
+        const f3 pos = k == 0 ? p0 : (k == 1 ? p1 : p2);
+        if (pos.z < 0.0f) F.z += P.Ks * fabsf(pos.z);
+        if (fabsf(pos.z) < range) {
+          const f3 c2v = mk(pos.x, pos.y, 0.0f) - C;
+          const float dd = sqrtf(0.0f * 0.0f + 0.0f * 0.0f + pos.z * pos.z);
+          const float ftmp = (float)((double)P.Ks * (1.0 - (double)(dd / P.l0)));
+          const f3 n = normalize(c2v);
+          F = F + mk(n.x * ftmp, n.y * ftmp, n.z * ftmp);
+        }
+      }
+    }
+    // triangle bending, vertex gather (extension)
+    if (bend) {
+      for (int e = e0; e < e1; ++e) {
+        const int f = a.mesh.inc_face[e], k = a.mesh.inc_corner[e];
+        const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
+                 p2 = vtx(s, s.faces[3 * f + 2]);
+        const f3 G = mk(s.bgx[f], s.bgy[f], s.bgz[f]);
+        const f3 t = k == 0 ? cross(p1 - p2, G) : (k == 1 ? cross(p2 - p0, G) : cross(G, p1 - p0));
+        F = F + P.Kb * t;
+      }
+    }
+    s.fx[v] = F.x;
+    s.fy[v] = F.y;
+    s.fz[v] = F.z;
+  }
+  __syncthreads();
+
+  // RepellingForces (Cell3D_Kernel.cl:251-310) over the neighbour list
+  if (T.Kre != 0.0f) {
+    const int nnc = a.nn[c];
+    const bool scan_all =
+        nnc == kNbOverflow || *((volatile const int *)(a.stale + P.tissue)) != 0;
+    const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
+    const int *list = a.nbr + (size_t)c * kMaxNB3D;
+    const float L = T.L;
+    const float four_pi = 4.0f * (float)M_PI;
+    for (int q = 0; q < count; ++q) {
+      const int j = scan_all ? T.cell_begin + q : list[q];
+      if (j == c) continue;
+      const Geom3D gj = a.geom_in[j];
+      f3 shift = mk(0.f, 0.f, 0.f);
+      if (T.pbc) {
+        shift = mk(__fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cx, gj.cx), L))),
+                   __fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cy, gj.cy), L))),
+                   __fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cz, gj.cz), L))));
+      }
+      const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
+      const f3 dc = C - cj;
+      const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
+                        fabsf(C.z);
+      const float rr = gi.R + gj.R + 1e-4f * (gi.R + gj.R) + 1e-5f * mag;
+      if (!(dot(dc, dc) <= rr * rr)) continue;
+      if (tid == 0) *s.ncand = 0;
+      __syncthreads();
+      const float rj = gj.R * (1.0f + 1e-4f) + 1e-5f * mag;
+      for (int v = tid; v < NV; v += kThreads) {
+        const f3 d = vtx(s, v) - cj;
+        if (dot(d, d) <= rj * rj) s.cand[atomicAdd(s.ncand, 1)] = (uint16_t)v;
+      }
+      __syncthreads();
+      const int ncand = *s.ncand;
+      if (ncand > 0) {
+        const size_t bj = (size_t)j * NV;
+        for (int k = tid; k < NV; k += kThreads) {
+          s.qx[k] = a.xin[bj + k] + shift.x;
+          s.qy[k] = a.yin[bj + k] + shift.y;
+          s.qz[k] = a.zin[bj + k] + shift.z;
+        }
+        __syncthreads();
+        float *ux = s.ux + w * NV, *uy = s.uy + w * NV, *uz = s.uz + w * NV;
+        for (int i = w; i < ncand; i += kWarps) {
+          const int v = s.cand[i];
+          const f3 pt = vtx(s, v);
+          for (int k = lane; k < NV; k += 32) {
+            const f3 u = normalize(mk(s.qx[k], s.qy[k], s.qz[k]) - pt);
+            ux[k] = u.x;
+            uy[k] = u.y;
+            uz[k] = u.z;
+          }
+          __syncwarp();
+          float part = 0.0f;
+          for (int f = lane; f < NF; f += 32) {
+            const int i0 = s.faces[3 * f], i1 = s.faces[3 * f + 1], i2 = s.faces[3 * f + 2];
+            const f3 u = mk(ux[i0], uy[i0], uz[i0]), vv = mk(ux[i1], uy[i1], uz[i1]),
+                     ww = mk(ux[i2], uy[i2], uz[i2]);
+            const float denom = 1.0f + dot(u, vv) + dot(vv, ww) + dot(ww, u);
+            if (denom < 1e-8f) continue;
+            const float num = dot(u, cross(vv, ww));
+            part += 2.0f * atan2f(num, denom);
+          }
+          const float wn = warp_sum(part) / four_pi;
+          if (lane == 0 && !(fabsf(wn) < 1e-6f)) {
+            const f3 dir = normalize(C - pt);
+            const float sc = fabsf(wn) * 0.5f * T.Kre;
+            s.fx[v] += sc * dir.x;
+            s.fy[v] += sc * dir.y;
+            s.fz[v] += sc * dir.z;
+            s.wnc[v] = (unsigned char)min(255, s.wnc[v] + 1);
+          }
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // EulerPosition (Cell3D_Kernel.cl:371-381) and outputs
+  for (int v = tid; v < NV; v += kThreads) {
+    const float nx = __fadd_rn(s.px[v], __fmul_rn(s.fx[v], a.dt));
+    const float ny = __fadd_rn(s.py[v], __fmul_rn(s.fy[v], a.dt));
+    const float nz = __fadd_rn(s.pz[v], __fmul_rn(s.fz[v], a.dt));
+    a.xout[base + v] = nx;
+    a.yout[base + v] = ny;
+    a.zout[base + v] = nz;
+    if (a.fx) {
+      a.fx[base + v] = s.fx[v];
+      a.fy[base + v] = s.fy[v];
+      a.fz[base + v] = s.fz[v];
+    }
+    if (a.wn_out) a.wn_out[base + v] = s.wnc[v];
+    s.px[v] = nx;
+    s.py[v] = ny;
+    s.pz[v] = nz;
+  }
+  __syncthreads();
+  const Geom3D g = mesh_geom(s.px, s.py, s.pz, NV, s.red);
+  if (tid == 0) {
+    a.geom_out[c] = g;
+    if (!(isfinite(g.cx) && isfinite(g.cy) && isfinite(g.cz) && isfinite(g.R)))
+      atomicOr(a.err, 1);
+    const Geom3D g0 = a.geom0[c];
+    const float dx = g.cx - g0.cx, dy = g.cy - g0.cy, dz = g.cz - g0.cz;
+    const float d = sqrtf(dx * dx + dy * dy + dz * dz) + fmaxf(0.0f, g.R - g0.R);
+    if (!(d <= 0.5f * T.skin)) atomicOr(a.stale + P.tissue, 1);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k3d_geom(const float *x, const float *y, const float *z, Geom3D *geom, int nv) {
+  __shared__ float px[kMaxNV3D], py[kMaxNV3D], pz[kMaxNV3D], red[64];
+  const size_t base = (size_t)blockIdx.x * nv;
+  for (int v = threadIdx.x; v < nv; v += kThreads) {
+    px[v] = x[base + v];
+    py[v] = y[base + v];
+    pz[v] = z[base + v];
+  }
+  __syncthreads();
+  const Geom3D g = mesh_geom(px, py, pz, nv, red);
+  if (threadIdx.x == 0) geom[blockIdx.x] = g;
+}
+
+// ---------------------------------------------------------------------------
+// Cell list (3D): periodic bins of the centres, sorted keys, neighbour lists
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int bin3(float x, float L, float inv, int nb) {
+  const float wx = __fsub_rn(x, __fmul_rn(L, floorf(__fdiv_rn(x, L))));
+  const int b = (int)floorf(__fmul_rn(wx, inv));
+  return max(0, min(b, nb - 1));
+}
+
+__global__ void __launch_bounds__(256) k3d_binprep(Rebuild3DArgs a, int local_bits) {
+  __shared__ float red[64];
+  const int t = blockIdx.x;
+  const Tissue3D T = a.tissues[t];
+  float dmax = 0.0f;
+  for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x)
+    dmax = fmaxf(dmax, 2.0f * a.geom[c].R);
+  dmax = warp_max(dmax);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmax;
+  __syncthreads();
+  float m = 0.0f;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmaxf(m, red[i]);
+  float wdt = __fadd_rn(__fadd_rn(m, T.skin), __fadd_rn(__fmul_rn(1e-3f, m), __fmul_rn(1e-5f, T.L)));
+  int nb = (int)floorf(__fdiv_rn(T.L, wdt));
+  nb = max(1, min(nb, T.cap));
+  if (threadIdx.x == 0) {
+    a.tissues[t].nb = nb;
+    a.tissues[t].binw = wdt;
+    a.stale[t] = 0;
+  }
+  const float inv = __fdiv_rn((float)nb, T.L);
+  for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x) {
+    const Geom3D g = a.geom[c];
+    const int bx = bin3(g.cx, T.L, inv, nb), by = bin3(g.cy, T.L, inv, nb),
+              bz = bin3(g.cz, T.L, inv, nb);
+    a.keys[c] = ((uint32_t)t << local_bits) | (uint32_t)((bz * nb + by) * nb + bx);
+    a.vals[c] = (uint32_t)c;
+  }
+}
+
+constexpr int kNb3Warps = 8;
+constexpr int kNb3Buf = 128;
+
+__device__ __forceinline__ int lb_u32(const uint32_t *a, int lo, int hi, uint32_t key) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool pair3(const Geom3D &gi, const Geom3D &gj, const Tissue3D &T) {
+  float dx = __fsub_rn(gi.cx, gj.cx), dy = __fsub_rn(gi.cy, gj.cy), dz = __fsub_rn(gi.cz, gj.cz);
+  if (T.pbc) {
+    dx = __fsub_rn(dx, __fmul_rn(T.L, roundf(__fdiv_rn(dx, T.L))));
+    dy = __fsub_rn(dy, __fmul_rn(T.L, roundf(__fdiv_rn(dy, T.L))));
+    dz = __fsub_rn(dz, __fmul_rn(T.L, roundf(__fdiv_rn(dz, T.L))));
+  }
+  const float mag = __fadd_rn(__fadd_rn(__fadd_rn(fabsf(gi.cx), fabsf(gi.cy)), fabsf(gi.cz)), T.L);
+  const float m = __fadd_rn(__fmul_rn(1e-3f, __fadd_rn(gi.R, gj.R)), __fmul_rn(1e-4f, mag));
+  const float r = __fadd_rn(__fadd_rn(__fadd_rn(gi.R, gj.R), T.skin), m);
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  return d2 <= __fmul_rn(r, r);
+}
+
+__global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a, int local_bits) {
+  __shared__ int buf[kNb3Warps][kNb3Buf];
+  __shared__ unsigned char uniq[kNb3Warps][kNb3Buf];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kNb3Warps + w;
+  if (c >= a.ncells) return;
+  const int t = (int)a.cells[c].tissue;
+  const Tissue3D T = a.tissues[t];
+  const Geom3D gi = a.geom[c];
+  const unsigned lt = (1u << lane) - 1u;
+  const int nb = T.nb;
+  const float inv = __fdiv_rn((float)nb, T.L);
+  const int bx = bin3(gi.cx, T.L, inv, nb), by = bin3(gi.cy, T.L, inv, nb),
+            bz = bin3(gi.cz, T.L, inv, nb);
+  const int lo_off = nb >= 3 ? -1 : 0, hi_off = nb >= 3 ? 1 : nb - 1;
+  int cnt = 0;
+  for (int oz = lo_off; oz <= hi_off; ++oz)
+    for (int oy = lo_off; oy <= hi_off; ++oy)
+      for (int ox = lo_off; ox <= hi_off; ++ox) {
+        const int xx = (bx + ox + nb) % nb, yy = (by + oy + nb) % nb, zz = (bz + oz + nb) % nb;
+        const uint32_t key = ((uint32_t)t << local_bits) | (uint32_t)((zz * nb + yy) * nb + xx);
+        const int lo = lb_u32(a.sorted_keys, T.cell_begin, T.cell_end, key);
+        const int hi = lb_u32(a.sorted_keys, lo, T.cell_end, key + 1u);
+        for (int b0 = lo; b0 < hi; b0 += 32) {
+          const int q = b0 + lane;
+          const int j = q < hi ? (int)a.sorted_vals[q] : -1;
+          const bool ok = j >= 0 && j != c && pair3(gi, a.geom[j], T);
+          const unsigned m = __ballot_sync(kFull, ok);
+          const int pos = cnt + __popc(m & lt);
+          if (ok && pos < kNb3Buf) buf[w][pos] = j;
+          cnt += __popc(m);
+        }
+      }
+  __syncwarp();
+  int nout;
+  if (cnt > kNb3Buf) {
+    nout = kNbOverflow;
+  } else {
+    for (int i = lane; i < cnt; i += 32) {
+      const int v = buf[w][i];
+      bool first = true;
+      for (int k = 0; k < i; ++k) first &= buf[w][k] != v;
+      uniq[w][i] = first ? 1 : 0;
+    }
+    __syncwarp();
+    int nu = 0;
+    for (int i = 0; i < cnt; ++i) nu += uniq[w][i];
+    if (nu > kMaxNB3D) {
+      nout = kNbOverflow;
+    } else {
+      int *out = a.nbr + (size_t)c * kMaxNB3D;
+      for (int i = lane; i < cnt; i += 32) {
+        if (!uniq[w][i]) continue;
+        const int v = buf[w][i];
+        int rank = 0;
+        for (int k = 0; k < cnt; ++k) rank += (uniq[w][k] && buf[w][k] < v) ? 1 : 0;
+        out[rank] = v;
+      }
+      nout = nu;
+    }
+  }
+  if (lane == 0) {
+    a.nn[c] = nout;
+    a.geom0[c] = gi;
+  }
+}
+
+} // namespace
+
+size_t step3d_smem_bytes(int nv, int nf, bool bend) {
+  size_t floats = (size_t)9 * nv + (size_t)3 * kWarps * nv + 64 + (bend ? (size_t)7 * nf : 0) + 4;
+  size_t halves = (size_t)3 * nf + nv;
+  return floats * 4 + halves * 2 + (size_t)nv + 16;
+}
+
+cudaError_t prepare_step3d(int nv, int nf, bool bend) {
+  const size_t bytes = step3d_smem_bytes(nv, nf, bend);
+  return cudaFuncSetAttribute(k3d_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {
+  const size_t bytes = step3d_smem_bytes(a.mesh.nv, a.mesh.nf, a.bend != 0);
+  k3d_step<<<a.ncells, kThreads, bytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_geom3d(const float *x, const float *y, const float *z, Geom3D *geom,
+                          int ncells, int nv, cudaStream_t s) {
+  k3d_geom<<<ncells, kThreads, 0, s>>>(x, y, z, geom, nv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s) {
+  k3d_binprep<<<a.ntissues, 256, 0, s>>>(a, local_bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s) {
+  k3d_neighbors<<<(a.ncells + kNb3Warps - 1) / kNb3Warps, kNb3Warps * 32, 0, s>>>(a, local_bits);
+  return cudaGetLastError();
+}
+
+} // namespace dpm

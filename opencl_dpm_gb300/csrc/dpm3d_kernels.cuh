@@ -1,0 +1,55 @@
+// 3D DPM kernels: launch interface.
+#pragma once
+
+#include "dpm_common.cuh"
+
+namespace dpm {
+
+// Mesh topology shared by every cell of a 3D batch.
+struct Mesh3D {
+  int nv, nf;
+  const uint16_t *faces;    // [nf*3] vertex ids
+  const int *inc_off;       // [nv+1] CSR offsets: faces around each vertex
+  const uint16_t *inc_face; // [3*nf] face ids, ascending per vertex
+  const uint8_t *inc_corner;// [3*nf] corner (0..2) of the vertex in that face
+  const int16_t *adj;       // [nf*3] face across edge e (vertices e, e+1), -1 none
+};
+
+struct Step3DArgs {
+  Mesh3D mesh;
+  const Cell3D *cells;
+  const Tissue3D *tissues;
+  const float *xin, *yin, *zin;  // positions (SoA, cell-major)
+  float *xout, *yout, *zout;
+  float *fx, *fy, *fz;           // forces of this step, or nullptr
+  unsigned char *wn_out;         // winding hits of this step, or nullptr
+  const Geom3D *geom_in;
+  Geom3D *geom_out;
+  const Geom3D *geom0;
+  const int *nn, *nbr;
+  int *stale, *err;
+  int ncells;
+  float dt;
+  int bend; // any cell with Kb != 0
+};
+
+struct Rebuild3DArgs {
+  const Cell3D *cells;
+  Tissue3D *tissues;
+  const Geom3D *geom;
+  Geom3D *geom0;
+  uint32_t *keys, *vals;
+  const uint32_t *sorted_keys, *sorted_vals;
+  int *nn, *nbr, *stale;
+  int ncells, ntissues;
+};
+
+cudaError_t launch_geom3d(const float *x, const float *y, const float *z, Geom3D *geom,
+                          int ncells, int nv, cudaStream_t s);
+cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
+cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
+size_t step3d_smem_bytes(int nv, int nf, bool bend);
+cudaError_t prepare_step3d(int nv, int nf, bool bend);
+cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s);
+
+} // namespace dpm

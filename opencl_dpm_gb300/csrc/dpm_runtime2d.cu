@@ -1,0 +1,607 @@
+// Runtime of the 2D path: context, batch objects, captured step graphs and
+// the C ABI declared in include/dpm_gb300.h.
+//
+// A call dpm2d_step(b, n, dt) runs n steps as blocks of `rebuild_period`
+// steps.  Each block is one CUDA graph: the cell-list rebuild (per-tissue
+// bins and keys, a stable device radix sort of the keys, neighbour lists)
+// followed by `rebuild_period` launches of the fused step kernel, the last
+// of which also stores the forces and containment flags when it ends the
+// call.  Graphs are instantiated once per (block length, parity, dt, last)
+// and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "dpm2d_kernels.cuh"
+#include "dpm_common.cuh"
+#include "dpm_runtime.hpp"
+#include "radix_sort.cuh"
+
+namespace dpm {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+  g_last_error = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+  return DPM_ECUDA;
+}
+const char *last_error() { return g_last_error.c_str(); }
+
+static int ceil_log2(long v) {
+  int b = 0;
+  while ((1L << b) < v) ++b;
+  return b;
+}
+
+} // namespace dpm
+
+using namespace dpm;
+
+struct dpm2d_batch {
+  dpm_ctx *ctx = nullptr;
+  int ntissues = 0, ncells = 0, maxnv = 0;
+  long nverts = 0;
+  std::vector<int> tissue_ncells;
+  std::vector<unsigned> nv;
+  std::vector<uint32_t> voff;
+  std::vector<Cell2D> h_cells;
+  std::vector<Tissue2D> h_tissues;
+  bool cells_set = false, tissues_set = false, uploaded = false;
+
+  DeviceArena arena;
+  Cell2D *d_cells = nullptr;
+  Tissue2D *d_tissues = nullptr;
+  float2 *d_pos[2] = {nullptr, nullptr};
+  float2 *d_force = nullptr;
+  unsigned char *d_flags = nullptr;
+  Geom2D *d_geom[2] = {nullptr, nullptr};
+  Geom2D *d_geom0 = nullptr;
+  int *d_nn = nullptr, *d_nbr = nullptr, *d_stale = nullptr, *d_err = nullptr;
+  uint32_t *d_keys = nullptr, *d_vals = nullptr, *d_keys_alt = nullptr, *d_vals_alt = nullptr;
+  uint32_t *d_sort_scratch = nullptr;
+  int cur = 0;
+  int local_bits = 1, key_bits = 1;
+  bool sorted_in_alt = false;
+
+  int rebuild_period = 16;
+  float skin_rel = 0.15f;
+  int warps = 8;
+  long rebuilds = 0;
+
+  std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
+
+  ~dpm2d_batch() { clear_graphs(); }
+  void clear_graphs() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+
+  Rebuild2DArgs rebuild_args() const {
+    Rebuild2DArgs a{};
+    a.cells = d_cells;
+    a.tissues = d_tissues;
+    a.geom = d_geom[cur];
+    a.geom0 = d_geom0;
+    a.keys = d_keys;
+    a.vals = d_vals;
+    a.sorted_keys = sorted_in_alt ? d_keys_alt : d_keys;
+    a.sorted_vals = sorted_in_alt ? d_vals_alt : d_vals;
+    a.nn = d_nn;
+    a.nbr = d_nbr;
+    a.stale = d_stale;
+    a.ncells = ncells;
+    a.ntissues = ntissues;
+    return a;
+  }
+
+  // Enqueue one neighbour-list rebuild on geometry buffer `g`.
+  cudaError_t enqueue_rebuild(int g, cudaStream_t s) {
+    Rebuild2DArgs a = rebuild_args();
+    a.geom = d_geom[g];
+    cudaError_t e = launch_binprep2d(a, local_bits, s);
+    if (e != cudaSuccess) return e;
+    bool alt = false;
+    e = radix_sort_pairs(d_keys, d_vals, d_keys_alt, d_vals_alt, ncells, key_bits,
+                         d_sort_scratch, s, &alt);
+    if (e != cudaSuccess) return e;
+    sorted_in_alt = alt;
+    a.sorted_keys = alt ? d_keys_alt : d_keys;
+    a.sorted_vals = alt ? d_vals_alt : d_vals;
+    return launch_neighbors2d(a, local_bits, s);
+  }
+
+  Step2DArgs step_args(int from, float dt, bool last) const {
+    Step2DArgs a{};
+    a.cells = d_cells;
+    a.tissues = d_tissues;
+    a.pos_in = d_pos[from];
+    a.pos_out = d_pos[1 - from];
+    a.force_out = last ? d_force : nullptr;
+    a.flags_out = last ? d_flags : nullptr;
+    a.geom_in = d_geom[from];
+    a.geom_out = d_geom[1 - from];
+    a.geom0 = d_geom0;
+    a.nn = d_nn;
+    a.nbr = d_nbr;
+    a.stale = d_stale;
+    a.err = d_err;
+    a.ncells = ncells;
+    a.dt = dt;
+    return a;
+  }
+
+  // Enqueue a block: rebuild, then `len` steps starting from buffer `from`.
+  cudaError_t enqueue_block(int len, int from, float dt, bool last, cudaStream_t s) {
+    cudaError_t e = enqueue_rebuild(from, s);
+    if (e != cudaSuccess) return e;
+    int f = from;
+    for (int i = 0; i < len; ++i) {
+      e = launch_step2d(step_args(f, dt, last && i == len - 1), maxnv, warps, s);
+      if (e != cudaSuccess) return e;
+      f = 1 - f;
+    }
+    return cudaSuccess;
+  }
+
+  int run_block(int len, float dt, bool last) {
+    cudaStream_t s = ctx->stream;
+    uint32_t dtbits;
+    std::memcpy(&dtbits, &dt, 4);
+    auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0);
+    auto it = graphs.find(key);
+    if (it == graphs.end()) {
+      cudaGraph_t g = nullptr;
+      DPM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = enqueue_block(len, cur, dt, last, s);
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e, "enqueue_block");
+      }
+      if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+      cudaGraphExec_t ex = nullptr;
+      e = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+      it = graphs.emplace(key, ex).first;
+    }
+    DPM_CUDA_TRY(cudaGraphLaunch(it->second, s));
+    if (len % 2) cur = 1 - cur;
+    ++rebuilds;
+    return DPM_OK;
+  }
+};
+
+namespace {
+
+int check_batch(dpm2d_batch *b) {
+  if (!b) return fail(DPM_EINVAL, "null batch");
+  return DPM_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *dpm_last_error(void) { return dpm::last_error(); }
+const char *dpm_version(void) { return "dpm_gb300 0.1 (sm_103a)"; }
+
+int dpm_ctx_create(int device, dpm_ctx **out) {
+  if (!out) return fail(DPM_EINVAL, "null output pointer");
+  *out = nullptr;
+  int n = 0;
+  DPM_CUDA_TRY(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(DPM_EINVAL, "no such CUDA device");
+  DPM_CUDA_TRY(cudaSetDevice(device));
+  auto *c = new (std::nothrow) dpm_ctx();
+  if (!c) return fail(DPM_ECAPACITY, "out of host memory");
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return DPM_OK;
+}
+
+int dpm_ctx_destroy(dpm_ctx *ctx) {
+  if (!ctx) return DPM_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return DPM_OK;
+}
+
+int dpm_ctx_synchronize(dpm_ctx *ctx) {
+  if (!ctx) return fail(DPM_EINVAL, "null context");
+  DPM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return DPM_OK;
+}
+
+int dpm_ctx_sm_count(dpm_ctx *ctx, int *out) {
+  if (!ctx || !out) return fail(DPM_EINVAL, "null argument");
+  *out = ctx->sm_count;
+  return DPM_OK;
+}
+
+int dpm_ctx_stream(dpm_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return fail(DPM_EINVAL, "null argument");
+  *stream = (void *)ctx->stream;
+  return DPM_OK;
+}
+
+int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *nv,
+                 dpm2d_batch **out) {
+  if (!ctx || !ncells || !nv || !out) return fail(DPM_EINVAL, "null argument");
+  *out = nullptr;
+  if (ntissues <= 0) return fail(DPM_EINVAL, "ntissues must be positive");
+  if (ntissues > 4096) return fail(DPM_ECAPACITY, "at most 4096 tissues per batch");
+  try {
+    auto b = std::make_unique<dpm2d_batch>();
+    b->ctx = ctx;
+    b->ntissues = ntissues;
+    long total_cells = 0;
+    for (int t = 0; t < ntissues; ++t) {
+      if (ncells[t] <= 0) return fail(DPM_EINVAL, "every tissue needs at least one cell");
+      total_cells += ncells[t];
+    }
+    if (total_cells > (1L << 26)) return fail(DPM_ECAPACITY, "too many cells");
+    b->ncells = (int)total_cells;
+    b->tissue_ncells.assign(ncells, ncells + ntissues);
+    b->nv.assign(nv, nv + total_cells);
+    b->voff.resize(total_cells);
+    long off = 0;
+    for (long c = 0; c < total_cells; ++c) {
+      if (nv[c] < 3 || nv[c] > (unsigned)kMaxNV2D)
+        return fail(DPM_EINVAL, "every cell needs 3..256 vertices");
+      b->voff[c] = (uint32_t)off;
+      off += nv[c];
+      b->maxnv = std::max(b->maxnv, (int)nv[c]);
+    }
+    if (off > (1L << 31) - 1) return fail(DPM_ECAPACITY, "too many vertices");
+    b->nverts = off;
+    b->h_cells.resize(total_cells);
+    b->h_tissues.resize(ntissues);
+    int cb = 0;
+    for (int t = 0; t < ntissues; ++t) {
+      Tissue2D &T = b->h_tissues[t];
+      std::memset(&T, 0, sizeof(T));
+      T.cell_begin = cb;
+      T.cell_end = cb + ncells[t];
+      T.cap = 1;
+      T.nbx = T.nby = 1;
+      for (int c = cb; c < cb + ncells[t]; ++c) {
+        Cell2D &C = b->h_cells[c];
+        std::memset(&C, 0, sizeof(C));
+        C.voff = b->voff[c];
+        C.nv = b->nv[c];
+        C.tissue = (uint32_t)t;
+      }
+      cb += ncells[t];
+    }
+    const long V = b->nverts, N = b->ncells;
+    DeviceArena &A = b->arena;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    e = A.reserve(sizeof(Cell2D) * N + sizeof(Tissue2D) * ntissues + 3 * sizeof(float2) * V +
+                  V + 3 * sizeof(Geom2D) * N + sizeof(int) * (N + N * kMaxNB2D) +
+                  sizeof(int) * (ntissues + 1) + 4 * sizeof(uint32_t) * N +
+                  radix_sort_scratch_bytes((int)N) + 64 * 256);
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation");
+    b->d_cells = A.take<Cell2D>(N);
+    b->d_tissues = A.take<Tissue2D>(ntissues);
+    b->d_pos[0] = A.take<float2>(V);
+    b->d_pos[1] = A.take<float2>(V);
+    b->d_force = A.take<float2>(V);
+    b->d_flags = A.take<unsigned char>(V);
+    b->d_geom[0] = A.take<Geom2D>(N);
+    b->d_geom[1] = A.take<Geom2D>(N);
+    b->d_geom0 = A.take<Geom2D>(N);
+    b->d_nn = A.take<int>(N);
+    b->d_nbr = A.take<int>(N * kMaxNB2D);
+    b->d_stale = A.take<int>(ntissues);
+    b->d_err = A.take<int>(1);
+    b->d_keys = A.take<uint32_t>(N);
+    b->d_vals = A.take<uint32_t>(N);
+    b->d_keys_alt = A.take<uint32_t>(N);
+    b->d_vals_alt = A.take<uint32_t>(N);
+    b->d_sort_scratch = A.take<uint32_t>(radix_sort_scratch_bytes((int)N) / 4 + 1);
+    if (!A.ok()) return fail(DPM_ECAPACITY, "device arena exhausted");
+    e = cudaMemsetAsync(A.base(), 0, A.used(), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    *out = b.release();
+    return DPM_OK;
+  } catch (const std::bad_alloc &) {
+    return fail(DPM_ECAPACITY, "out of host memory");
+  }
+}
+
+int dpm2d_destroy(dpm2d_batch *b) {
+  if (!b) return DPM_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  delete b;
+  return DPM_OK;
+}
+
+int dpm2d_sizes(dpm2d_batch *b, int *ncells, long *nvertices) {
+  if (int r = check_batch(b)) return r;
+  if (ncells) *ncells = b->ncells;
+  if (nvertices) *nvertices = b->nverts;
+  return DPM_OK;
+}
+
+int dpm2d_set_cells(dpm2d_batch *b, const float *Ka, const float *Kl, const float *Kb,
+                    const float *a0, const float *l0, const float *r0) {
+  if (int r = check_batch(b)) return r;
+  if (!Ka || !Kl || !Kb || !a0 || !l0 || !r0) return fail(DPM_EINVAL, "null parameter array");
+  for (int c = 0; c < b->ncells; ++c) {
+    if (!(a0[c] > 0.0f) || !(l0[c] > 0.0f) || !(r0[c] > 0.0f))
+      return fail(DPM_EINVAL, "a0, l0 and r0 must be positive");
+    Cell2D &C = b->h_cells[c];
+    C.a0 = a0[c];
+    C.l0 = l0[c];
+    // the reference forms these in float (Cell2D_kernel.cl:38, :118)
+    C.kA = Ka[c] / std::sqrt(a0[c]);
+    C.kL = Kl[c] * std::sqrt(a0[c] / l0[c]);
+    C.Kb = Kb[c];
+    C.r0 = r0[c];
+  }
+  // attraction range, skin and bin cap depend on the cells of each tissue
+  for (int t = 0; t < b->ntissues; ++t) {
+    Tissue2D &T = b->h_tissues[t];
+    float l0max = 0.0f, a0max = 0.0f;
+    double rsum = 0.0;
+    for (int c = T.cell_begin; c < T.cell_end; ++c) {
+      l0max = std::max(l0max, b->h_cells[c].l0);
+      a0max = std::max(a0max, b->h_cells[c].a0);
+      rsum += b->h_cells[c].r0;
+    }
+    T.l0max = l0max;
+    T.skin = (float)(b->skin_rel * 2.0 * rsum / (T.cell_end - T.cell_begin));
+  }
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells, b->h_cells.data(), sizeof(Cell2D) * b->ncells,
+                               cudaMemcpyHostToDevice, b->ctx->stream));
+  b->cells_set = true;
+  if (b->tissues_set) {
+    DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
+                                 sizeof(Tissue2D) * b->ntissues, cudaMemcpyHostToDevice,
+                                 b->ctx->stream));
+  }
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return DPM_OK;
+}
+
+int dpm2d_set_tissues(dpm2d_batch *b, const float *L, const float *Kre, const float *Kat,
+                      const int *pbc) {
+  if (int r = check_batch(b)) return r;
+  if (!L || !Kre || !Kat || !pbc) return fail(DPM_EINVAL, "null parameter array");
+  int max_local = 1;
+  for (int t = 0; t < b->ntissues; ++t) {
+    if (!(L[t] > 0.0f) || !std::isfinite(L[t])) return fail(DPM_EINVAL, "L must be positive");
+    Tissue2D &T = b->h_tissues[t];
+    T.L = L[t];
+    T.Kre = Kre[t];
+    T.Kat = Kat[t];
+    T.pbc = pbc[t] ? 1 : 0;
+    // bins per axis never need to be narrower than a cell radius
+    float a0max = 0.0f;
+    for (int c = T.cell_begin; c < T.cell_end; ++c) a0max = std::max(a0max, b->h_cells[c].a0);
+    const double rad = a0max > 0.0f ? std::sqrt(a0max / M_PI) : 0.5;
+    long cap = (long)std::floor(L[t] / std::max(rad, 1e-6));
+    cap = std::max(1L, std::min(cap, (long)kMaxBinsAxis));
+    T.cap = (int)cap;
+    max_local = std::max(max_local, ceil_log2(cap * cap));
+  }
+  b->local_bits = std::max(1, max_local);
+  b->key_bits = b->local_bits + ceil_log2(b->ntissues);
+  if (b->key_bits > 32) return fail(DPM_ECAPACITY, "cell-list keys exceed 32 bits");
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue2D) * b->ntissues,
+                               cudaMemcpyHostToDevice, b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  b->tissues_set = true;
+  b->clear_graphs();
+  return DPM_OK;
+}
+
+int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel, int warps_per_block) {
+  if (int r = check_batch(b)) return r;
+  if (rebuild_period > 0) {
+    if (rebuild_period % 2) return fail(DPM_EINVAL, "rebuild period must be even");
+    b->rebuild_period = rebuild_period;
+  }
+  if (skin_rel > 0.0f) b->skin_rel = skin_rel;
+  if (warps_per_block > 0) {
+    if (warps_per_block != 4 && warps_per_block != 8 && warps_per_block != 16)
+      return fail(DPM_EINVAL, "warps per block must be 4, 8 or 16");
+    b->warps = warps_per_block;
+  }
+  b->clear_graphs();
+  if (b->cells_set && skin_rel > 0.0f) {
+    for (int t = 0; t < b->ntissues; ++t) {
+      Tissue2D &T = b->h_tissues[t];
+      double rsum = 0.0;
+      for (int c = T.cell_begin; c < T.cell_end; ++c) rsum += b->h_cells[c].r0;
+      T.skin = (float)(b->skin_rel * 2.0 * rsum / (T.cell_end - T.cell_begin));
+    }
+    if (b->tissues_set) {
+      cudaSetDevice(b->ctx->device);
+      DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
+                                   sizeof(Tissue2D) * b->ntissues, cudaMemcpyHostToDevice,
+                                   b->ctx->stream));
+      DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    }
+  }
+  return DPM_OK;
+}
+
+int dpm2d_upload(dpm2d_batch *b, const float *xy) {
+  if (int r = check_batch(b)) return r;
+  if (!xy) return fail(DPM_EINVAL, "null positions");
+  if (!b->cells_set) return fail(DPM_ESTATE, "set the cell constants before uploading");
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->ctx->stream;
+  b->cur = 0;
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_pos[0], xy, sizeof(float2) * b->nverts,
+                               cudaMemcpyHostToDevice, s));
+  DPM_CUDA_TRY(cudaMemsetAsync(b->d_force, 0, sizeof(float2) * b->nverts, s));
+  DPM_CUDA_TRY(cudaMemsetAsync(b->d_flags, 0, b->nverts, s));
+  DPM_CUDA_TRY(cudaMemsetAsync(b->d_err, 0, sizeof(int), s));
+  DPM_CUDA_TRY(launch_geom2d(b->d_cells, b->d_pos[0], b->d_geom[0], b->ncells, b->maxnv, s));
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  b->uploaded = true;
+  return DPM_OK;
+}
+
+int dpm2d_step_kernel(dpm2d_batch *b, float dt) {
+  if (int r = check_batch(b)) return r;
+  if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before stepping");
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true), b->maxnv, b->warps, b->ctx->stream));
+  b->cur = 1 - b->cur;
+  return DPM_OK;
+}
+
+int dpm2d_step(dpm2d_batch *b, int nsteps, float dt) {
+  if (int r = check_batch(b)) return r;
+  if (nsteps < 0) return fail(DPM_EINVAL, "nsteps must be non-negative");
+  if (!b->uploaded || !b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues and upload positions before stepping");
+  if (!std::isfinite(dt)) return fail(DPM_EINVAL, "dt must be finite");
+  if (nsteps == 0) return DPM_OK;
+  cudaSetDevice(b->ctx->device);
+  const int R = b->rebuild_period;
+  const int full = nsteps / R, rem = nsteps % R;
+  for (int i = 0; i < full; ++i)
+    if (int r = b->run_block(R, dt, rem == 0 && i == full - 1)) return r;
+  if (rem)
+    if (int r = b->run_block(rem, dt, true)) return r;
+  return DPM_OK;
+}
+
+int dpm2d_download(dpm2d_batch *b, float *xy, float *F) {
+  if (int r = check_batch(b)) return r;
+  if (!b->uploaded) return fail(DPM_ESTATE, "nothing uploaded");
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->ctx->stream;
+  if (xy)
+    DPM_CUDA_TRY(cudaMemcpyAsync(xy, b->d_pos[b->cur], sizeof(float2) * b->nverts,
+                                 cudaMemcpyDeviceToHost, s));
+  if (F)
+    DPM_CUDA_TRY(cudaMemcpyAsync(F, b->d_force, sizeof(float2) * b->nverts,
+                                 cudaMemcpyDeviceToHost, s));
+  int err = 0;
+  DPM_CUDA_TRY(cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (err & 1) return fail(DPM_ENONFINITE, "non-finite vertex positions");
+  return DPM_OK;
+}
+
+int dpm2d_last_contained(dpm2d_batch *b, unsigned char *flags) {
+  if (int r = check_batch(b)) return r;
+  if (!flags) return fail(DPM_EINVAL, "null output");
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(flags, b->d_flags, b->nverts, cudaMemcpyDeviceToHost,
+                               b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return DPM_OK;
+}
+
+int dpm2d_cell_areas(dpm2d_batch *b, float *area) {
+  if (int r = check_batch(b)) return r;
+  if (!area) return fail(DPM_EINVAL, "null output");
+  std::vector<Geom2D> g(b->ncells);
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(g.data(), b->d_geom[b->cur], sizeof(Geom2D) * b->ncells,
+                               cudaMemcpyDeviceToHost, b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  for (int c = 0; c < b->ncells; ++c) area[c] = g[c].area;
+  return DPM_OK;
+}
+
+int dpm2d_stats(dpm2d_batch *b, long *rebuilds, long *fallback_steps) {
+  if (int r = check_batch(b)) return r;
+  if (rebuilds) *rebuilds = b->rebuilds;
+  if (fallback_steps) {
+    std::vector<int> st(b->ntissues);
+    cudaSetDevice(b->ctx->device);
+    DPM_CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_stale, sizeof(int) * b->ntissues,
+                                 cudaMemcpyDeviceToHost, b->ctx->stream));
+    DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    long n = 0;
+    for (int v : st) n += v ? 1 : 0;
+    *fallback_steps = n;
+  }
+  return DPM_OK;
+}
+
+int dpm2d_rebuild_now(dpm2d_batch *b) {
+  if (int r = check_batch(b)) return r;
+  if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before rebuilding");
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(b->enqueue_rebuild(b->cur, b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return DPM_OK;
+}
+
+int dpm2d_cell_list(dpm2d_batch *b, unsigned *keys, unsigned *ids, int *nn, int *nbr,
+                    int *maxnb, float *geom) {
+  if (int r = check_batch(b)) return r;
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->ctx->stream;
+  const size_t N = b->ncells;
+  if (keys)
+    DPM_CUDA_TRY(cudaMemcpyAsync(keys, b->sorted_in_alt ? b->d_keys_alt : b->d_keys,
+                                 4 * N, cudaMemcpyDeviceToHost, s));
+  if (ids)
+    DPM_CUDA_TRY(cudaMemcpyAsync(ids, b->sorted_in_alt ? b->d_vals_alt : b->d_vals, 4 * N,
+                                 cudaMemcpyDeviceToHost, s));
+  if (nn) DPM_CUDA_TRY(cudaMemcpyAsync(nn, b->d_nn, 4 * N, cudaMemcpyDeviceToHost, s));
+  if (nbr)
+    DPM_CUDA_TRY(cudaMemcpyAsync(nbr, b->d_nbr, 4 * N * kMaxNB2D, cudaMemcpyDeviceToHost, s));
+  if (geom)
+    DPM_CUDA_TRY(cudaMemcpyAsync(geom, b->d_geom[b->cur], sizeof(Geom2D) * N,
+                                 cudaMemcpyDeviceToHost, s));
+  if (maxnb) *maxnb = kMaxNB2D;
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  return DPM_OK;
+}
+
+int dpm2d_bins(dpm2d_batch *b, int *local_bits, int *nbins, float *binw, float *skin) {
+  if (int r = check_batch(b)) return r;
+  std::vector<Tissue2D> T(b->ntissues);
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(T.data(), b->d_tissues, sizeof(Tissue2D) * b->ntissues,
+                               cudaMemcpyDeviceToHost, b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  if (local_bits) *local_bits = b->local_bits;
+  for (int t = 0; t < b->ntissues; ++t) {
+    if (nbins) nbins[t] = T[t].nbx;
+    if (binw) binw[t] = T[t].binw;
+    if (skin) skin[t] = T[t].skin;
+  }
+  return DPM_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,503 @@
+// Runtime of the 3D path: batch objects, mesh tables, captured step graphs
+// and the dpm3d_* entry points of include/dpm_gb300.h.
+//
+// The mesh topology is shared by every cell (the reference uploads cell 0's
+// face table for all cells, src/Tissue3D.cpp:144-146).  At creation the
+// host derives from it the vertex -> (face, corner) incidence lists sorted
+// by face id, which let each vertex gather its face terms in the order the
+// reference's atomics deliver them, and the face adjacency used by the
+// bending extension.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <tuple>
+#include <vector>
+
+#include "dpm3d_kernels.cuh"
+#include "dpm_common.cuh"
+#include "dpm_runtime.hpp"
+#include "radix_sort.cuh"
+
+using namespace dpm;
+
+namespace {
+int ceil_log2l(long v) {
+  int b = 0;
+  while ((1L << b) < v) ++b;
+  return b;
+}
+} // namespace
+
+struct dpm3d_batch {
+  dpm_ctx *ctx = nullptr;
+  int ntissues = 0, ncells = 0, nv = 0, nf = 0;
+  long nverts = 0;
+  std::vector<Cell3D> h_cells;
+  std::vector<Tissue3D> h_tissues;
+  bool cells_set = false, tissues_set = false, uploaded = false, bend = false;
+  DeviceArena arena;
+  Mesh3D mesh{};
+  Cell3D *d_cells = nullptr;
+  Tissue3D *d_tissues = nullptr;
+  float *d_pos[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  float *d_f[3] = {nullptr, nullptr, nullptr};
+  unsigned char *d_wn = nullptr;
+  Geom3D *d_geom[2] = {nullptr, nullptr};
+  Geom3D *d_geom0 = nullptr;
+  int *d_nn = nullptr, *d_nbr = nullptr, *d_stale = nullptr, *d_err = nullptr;
+  uint32_t *d_keys = nullptr, *d_vals = nullptr, *d_keys_alt = nullptr, *d_vals_alt = nullptr;
+  uint32_t *d_scratch = nullptr;
+  int cur = 0;
+  int local_bits = 1, key_bits = 1;
+  int rebuild_period = 8;
+  float skin_rel = 0.1f;
+  std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
+
+  ~dpm3d_batch() { clear_graphs(); }
+
+  // skin = skin_rel * mean cell diameter of each tissue
+  void update_skin() {
+    for (int t = 0; t < ntissues; ++t) {
+      Tissue3D &T = h_tissues[t];
+      double vs = 0.0;
+      for (int c = T.cell_begin; c < T.cell_end; ++c) vs += std::cbrt(h_cells[c].v0);
+      T.skin = (float)(skin_rel * 2.0 * std::cbrt(3.0 / (4.0 * M_PI)) * vs /
+                       (T.cell_end - T.cell_begin));
+    }
+  }
+
+  void clear_graphs() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+
+  cudaError_t enqueue_rebuild(int g, cudaStream_t s) {
+    Rebuild3DArgs a{};
+    a.cells = d_cells;
+    a.tissues = d_tissues;
+    a.geom = d_geom[g];
+    a.geom0 = d_geom0;
+    a.keys = d_keys;
+    a.vals = d_vals;
+    a.nn = d_nn;
+    a.nbr = d_nbr;
+    a.stale = d_stale;
+    a.ncells = ncells;
+    a.ntissues = ntissues;
+    cudaError_t e = launch_binprep3d(a, local_bits, s);
+    if (e != cudaSuccess) return e;
+    bool alt = false;
+    e = radix_sort_pairs(d_keys, d_vals, d_keys_alt, d_vals_alt, ncells, key_bits, d_scratch, s,
+                         &alt);
+    if (e != cudaSuccess) return e;
+    a.sorted_keys = alt ? d_keys_alt : d_keys;
+    a.sorted_vals = alt ? d_vals_alt : d_vals;
+    return launch_neighbors3d(a, local_bits, s);
+  }
+
+  Step3DArgs step_args(int from, float dt, bool last) const {
+    Step3DArgs a{};
+    a.mesh = mesh;
+    a.cells = d_cells;
+    a.tissues = d_tissues;
+    a.xin = d_pos[from][0];
+    a.yin = d_pos[from][1];
+    a.zin = d_pos[from][2];
+    a.xout = d_pos[1 - from][0];
+    a.yout = d_pos[1 - from][1];
+    a.zout = d_pos[1 - from][2];
+    a.fx = last ? d_f[0] : nullptr;
+    a.fy = last ? d_f[1] : nullptr;
+    a.fz = last ? d_f[2] : nullptr;
+    a.wn_out = last ? d_wn : nullptr;
+    a.geom_in = d_geom[from];
+    a.geom_out = d_geom[1 - from];
+    a.geom0 = d_geom0;
+    a.nn = d_nn;
+    a.nbr = d_nbr;
+    a.stale = d_stale;
+    a.err = d_err;
+    a.ncells = ncells;
+    a.dt = dt;
+    a.bend = bend ? 1 : 0;
+    return a;
+  }
+
+  cudaError_t enqueue_block(int len, int from, float dt, bool last, cudaStream_t s) {
+    cudaError_t e = enqueue_rebuild(from, s);
+    if (e != cudaSuccess) return e;
+    int f = from;
+    for (int i = 0; i < len; ++i) {
+      e = launch_step3d(step_args(f, dt, last && i == len - 1), s);
+      if (e != cudaSuccess) return e;
+      f = 1 - f;
+    }
+    return cudaSuccess;
+  }
+
+  int run_block(int len, float dt, bool last) {
+    cudaStream_t s = ctx->stream;
+    uint32_t dtbits;
+    std::memcpy(&dtbits, &dt, 4);
+    auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0);
+    auto it = graphs.find(key);
+    if (it == graphs.end()) {
+      cudaGraph_t g = nullptr;
+      DPM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = enqueue_block(len, cur, dt, last, s);
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e, "enqueue_block (3D)");
+      }
+      if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+      cudaGraphExec_t ex = nullptr;
+      e = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+      it = graphs.emplace(key, ex).first;
+    }
+    DPM_CUDA_TRY(cudaGraphLaunch(it->second, s));
+    if (len % 2) cur = 1 - cur;
+    return DPM_OK;
+  }
+};
+
+namespace {
+int check3(dpm3d_batch *b) {
+  if (!b) return fail(DPM_EINVAL, "null batch");
+  return DPM_OK;
+}
+} // namespace
+
+extern "C" {
+
+int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
+                 const unsigned *faces, dpm3d_batch **out) {
+  if (!ctx || !ncells || !faces || !out) return fail(DPM_EINVAL, "null argument");
+  *out = nullptr;
+  if (ntissues <= 0) return fail(DPM_EINVAL, "ntissues must be positive");
+  if (ntissues > 4096) return fail(DPM_ECAPACITY, "at most 4096 tissues per batch");
+  if (nv < 4 || nf < 4) return fail(DPM_EINVAL, "a mesh needs at least 4 vertices and faces");
+  if (nv > kMaxNV3D)
+    return fail(DPM_ECAPACITY, "at most 642 vertices per 3D cell (icosphere level 3)");
+  try {
+    auto b = std::make_unique<dpm3d_batch>();
+    b->ctx = ctx;
+    b->ntissues = ntissues;
+    b->nv = nv;
+    b->nf = nf;
+    long total = 0;
+    for (int t = 0; t < ntissues; ++t) {
+      if (ncells[t] <= 0) return fail(DPM_EINVAL, "every tissue needs at least one cell");
+      total += ncells[t];
+    }
+    if (total * nv > (1L << 31) - 1) return fail(DPM_ECAPACITY, "too many vertices");
+    b->ncells = (int)total;
+    b->nverts = total * nv;
+    // mesh tables
+    std::vector<uint16_t> f16(3 * (size_t)nf);
+    std::vector<std::vector<std::pair<int, int>>> inc(nv);
+    for (int f = 0; f < nf; ++f)
+      for (int k = 0; k < 3; ++k) {
+        const unsigned v = faces[3 * f + k];
+        if (v >= (unsigned)nv) return fail(DPM_EINVAL, "face index out of range");
+        f16[3 * f + k] = (uint16_t)v;
+        inc[v].push_back({f, k});
+      }
+    std::vector<int> off(nv + 1, 0);
+    std::vector<uint16_t> incf;
+    std::vector<uint8_t> incc;
+    for (int v = 0; v < nv; ++v) {
+      std::sort(inc[v].begin(), inc[v].end());
+      off[v + 1] = off[v] + (int)inc[v].size();
+      for (auto &p : inc[v]) {
+        incf.push_back((uint16_t)p.first);
+        incc.push_back((uint8_t)p.second);
+      }
+    }
+    std::vector<int16_t> adj(3 * (size_t)nf, -1);
+    {
+      std::map<std::pair<unsigned, unsigned>, std::pair<int, int>> edges;
+      for (int f = 0; f < nf; ++f)
+        for (int e = 0; e < 3; ++e) {
+          const unsigned a = faces[3 * f + e], c = faces[3 * f + (e + 1) % 3];
+          auto key = std::make_pair(std::min(a, c), std::max(a, c));
+          auto it = edges.find(key);
+          if (it == edges.end()) {
+            edges.emplace(key, std::make_pair(f, e));
+          } else {
+            adj[3 * f + e] = (int16_t)it->second.first;
+            adj[3 * it->second.first + it->second.second] = (int16_t)f;
+          }
+        }
+    }
+    b->h_cells.resize(total);
+    b->h_tissues.resize(ntissues);
+    int cb = 0;
+    for (int t = 0; t < ntissues; ++t) {
+      Tissue3D &T = b->h_tissues[t];
+      std::memset(&T, 0, sizeof(T));
+      T.cell_begin = cb;
+      T.cell_end = cb + ncells[t];
+      T.cap = 1;
+      T.nb = 1;
+      for (int c = cb; c < cb + ncells[t]; ++c) {
+        std::memset(&b->h_cells[c], 0, sizeof(Cell3D));
+        b->h_cells[c].tissue = (uint32_t)t;
+      }
+      cb += ncells[t];
+    }
+    const long V = b->nverts, N = b->ncells;
+    DeviceArena &A = b->arena;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    e = A.reserve(sizeof(uint16_t) * 3 * nf + sizeof(int) * (nv + 1) + 3 * nf * 3 +
+                  sizeof(int16_t) * 3 * nf + sizeof(Cell3D) * N + sizeof(Tissue3D) * ntissues +
+                  9 * sizeof(float) * V + V + 3 * sizeof(Geom3D) * N +
+                  sizeof(int) * (N + N * kMaxNB3D + ntissues + 1) + 4 * sizeof(uint32_t) * N +
+                  radix_sort_scratch_bytes((int)N) + 64 * 256);
+    if (e != cudaSuccess) return cuda_fail(e, "device allocation");
+    uint16_t *d_faces = A.take<uint16_t>(3 * nf);
+    int *d_off = A.take<int>(nv + 1);
+    uint16_t *d_incf = A.take<uint16_t>(3 * nf);
+    uint8_t *d_incc = A.take<uint8_t>(3 * nf);
+    int16_t *d_adj = A.take<int16_t>(3 * nf);
+    b->d_cells = A.take<Cell3D>(N);
+    b->d_tissues = A.take<Tissue3D>(ntissues);
+    for (int p = 0; p < 2; ++p)
+      for (int k = 0; k < 3; ++k) b->d_pos[p][k] = A.take<float>(V);
+    for (int k = 0; k < 3; ++k) b->d_f[k] = A.take<float>(V);
+    b->d_wn = A.take<unsigned char>(V);
+    b->d_geom[0] = A.take<Geom3D>(N);
+    b->d_geom[1] = A.take<Geom3D>(N);
+    b->d_geom0 = A.take<Geom3D>(N);
+    b->d_nn = A.take<int>(N);
+    b->d_nbr = A.take<int>(N * kMaxNB3D);
+    b->d_stale = A.take<int>(ntissues);
+    b->d_err = A.take<int>(1);
+    b->d_keys = A.take<uint32_t>(N);
+    b->d_vals = A.take<uint32_t>(N);
+    b->d_keys_alt = A.take<uint32_t>(N);
+    b->d_vals_alt = A.take<uint32_t>(N);
+    b->d_scratch = A.take<uint32_t>(radix_sort_scratch_bytes((int)N) / 4 + 1);
+    if (!A.ok()) return fail(DPM_ECAPACITY, "device arena exhausted");
+    cudaStream_t s = ctx->stream;
+    e = cudaMemsetAsync(A.base(), 0, A.used(), s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_faces, f16.data(), 2 * f16.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_off, off.data(), 4 * off.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_incf, incf.data(), 2 * incf.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_incc, incc.data(), incc.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_adj, adj.data(), 2 * adj.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "mesh upload");
+    b->mesh = Mesh3D{nv, nf, d_faces, d_off, d_incf, d_incc, d_adj};
+    e = prepare_step3d(nv, nf, true);
+    if (e != cudaSuccess) return cuda_fail(e, "shared-memory opt-in");
+    *out = b.release();
+    return DPM_OK;
+  } catch (const std::bad_alloc &) {
+    return fail(DPM_ECAPACITY, "out of host memory");
+  }
+}
+
+int dpm3d_destroy(dpm3d_batch *b) {
+  if (!b) return DPM_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  delete b;
+  return DPM_OK;
+}
+
+int dpm3d_sizes(dpm3d_batch *b, int *ncells, long *nvertices) {
+  if (int r = check3(b)) return r;
+  if (ncells) *ncells = b->ncells;
+  if (nvertices) *nvertices = b->nverts;
+  return DPM_OK;
+}
+
+int dpm3d_set_cells(dpm3d_batch *b, const float *Kv, const float *Ka, const float *Ks,
+                    const float *v0, const float *a0, const float *l0, const float *Kb,
+                    const float *adh) {
+  if (int r = check3(b)) return r;
+  if (!Kv || !Ka || !Ks || !v0 || !a0 || !l0) return fail(DPM_EINVAL, "null parameter array");
+  bool bend = false;
+  for (int c = 0; c < b->ncells; ++c) {
+    if (!(l0[c] > 0.0f) || !(a0[c] >= 0.0f) || !(v0[c] > 0.0f))
+      return fail(DPM_EINVAL, "v0 and l0 must be positive");
+    Cell3D &C = b->h_cells[c];
+    C.Kv = Kv[c];
+    C.Ka = Ka[c];
+    C.Ks = Ks[c];
+    C.v0 = v0[c];
+    C.a0 = a0[c];
+    C.l0 = l0[c];
+    C.Kb = Kb ? Kb[c] : 0.0f;
+    C.adh = adh ? adh[c] : l0[c] * 2.0f;
+    // Cell3D_Kernel.cl:167, in the reference's order of operations
+    C.sa_scale = Ka[c] * std::sqrt(a0[c]) / l0[c] * 0.3f;
+    bend |= C.Kb != 0.0f;
+  }
+  b->update_skin();
+  if (bend != b->bend) b->clear_graphs();
+  b->bend = bend;
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells, b->h_cells.data(), sizeof(Cell3D) * b->ncells,
+                               cudaMemcpyHostToDevice, b->ctx->stream));
+  if (b->tissues_set)
+    DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
+                                 sizeof(Tissue3D) * b->ntissues, cudaMemcpyHostToDevice,
+                                 b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  b->cells_set = true;
+  return DPM_OK;
+}
+
+int dpm3d_set_tissues(dpm3d_batch *b, const float *L, const float *Kre, const int *pbc) {
+  if (int r = check3(b)) return r;
+  if (!L || !Kre || !pbc) return fail(DPM_EINVAL, "null parameter array");
+  int max_local = 1;
+  for (int t = 0; t < b->ntissues; ++t) {
+    if (!(L[t] > 0.0f) || !std::isfinite(L[t])) return fail(DPM_EINVAL, "L must be positive");
+    Tissue3D &T = b->h_tissues[t];
+    T.L = L[t];
+    T.Kre = Kre[t];
+    T.pbc = pbc[t] ? 1 : 0;
+    float v0max = 0.0f;
+    for (int c = T.cell_begin; c < T.cell_end; ++c) v0max = std::max(v0max, b->h_cells[c].v0);
+    const double rad = v0max > 0.0f ? std::cbrt(3.0 * v0max / (4.0 * M_PI)) : 0.5;
+    long cap = (long)std::floor(L[t] / std::max(rad, 1e-6));
+    cap = std::max(1L, std::min(cap, 64L));
+    T.cap = (int)cap;
+    max_local = std::max(max_local, ceil_log2l(cap * cap * cap));
+  }
+  b->local_bits = max_local;
+  b->key_bits = b->local_bits + ceil_log2l(b->ntissues);
+  if (b->key_bits > 32) return fail(DPM_ECAPACITY, "cell-list keys exceed 32 bits");
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue3D) * b->ntissues,
+                               cudaMemcpyHostToDevice, b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  b->tissues_set = true;
+  b->clear_graphs();
+  return DPM_OK;
+}
+
+int dpm3d_upload(dpm3d_batch *b, const float *xyz) {
+  if (int r = check3(b)) return r;
+  if (!xyz) return fail(DPM_EINVAL, "null positions");
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->ctx->stream;
+  // de-interleave on the host into the structure-of-arrays layout
+  const long V = b->nverts;
+  std::vector<float> soa(3 * (size_t)V);
+  for (long i = 0; i < V; ++i) {
+    soa[i] = xyz[3 * i];
+    soa[V + i] = xyz[3 * i + 1];
+    soa[2 * V + i] = xyz[3 * i + 2];
+  }
+  b->cur = 0;
+  for (int k = 0; k < 3; ++k)
+    DPM_CUDA_TRY(cudaMemcpyAsync(b->d_pos[0][k], soa.data() + k * V, sizeof(float) * V,
+                                 cudaMemcpyHostToDevice, s));
+  for (int k = 0; k < 3; ++k) DPM_CUDA_TRY(cudaMemsetAsync(b->d_f[k], 0, sizeof(float) * V, s));
+  DPM_CUDA_TRY(cudaMemsetAsync(b->d_wn, 0, V, s));
+  DPM_CUDA_TRY(cudaMemsetAsync(b->d_err, 0, sizeof(int), s));
+  DPM_CUDA_TRY(launch_geom3d(b->d_pos[0][0], b->d_pos[0][1], b->d_pos[0][2], b->d_geom[0],
+                             b->ncells, b->nv, s));
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  b->uploaded = true;
+  return DPM_OK;
+}
+
+int dpm3d_step(dpm3d_batch *b, int nsteps, float dt) {
+  if (int r = check3(b)) return r;
+  if (nsteps < 0) return fail(DPM_EINVAL, "nsteps must be non-negative");
+  if (!b->uploaded || !b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues and upload positions before stepping");
+  if (!std::isfinite(dt)) return fail(DPM_EINVAL, "dt must be finite");
+  if (nsteps == 0) return DPM_OK;
+  cudaSetDevice(b->ctx->device);
+  const int R = b->rebuild_period;
+  const int full = nsteps / R, rem = nsteps % R;
+  for (int i = 0; i < full; ++i)
+    if (int r = b->run_block(R, dt, rem == 0 && i == full - 1)) return r;
+  if (rem)
+    if (int r = b->run_block(rem, dt, true)) return r;
+  return DPM_OK;
+}
+
+int dpm3d_download(dpm3d_batch *b, float *xyz, float *F) {
+  if (int r = check3(b)) return r;
+  if (!b->uploaded) return fail(DPM_ESTATE, "nothing uploaded");
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->ctx->stream;
+  const long V = b->nverts;
+  std::vector<float> soa(3 * (size_t)V);
+  int err = 0;
+  if (xyz)
+    for (int k = 0; k < 3; ++k)
+      DPM_CUDA_TRY(cudaMemcpyAsync(soa.data() + k * V, b->d_pos[b->cur][k], sizeof(float) * V,
+                                   cudaMemcpyDeviceToHost, s));
+  DPM_CUDA_TRY(cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (xyz)
+    for (long i = 0; i < V; ++i) {
+      xyz[3 * i] = soa[i];
+      xyz[3 * i + 1] = soa[V + i];
+      xyz[3 * i + 2] = soa[2 * V + i];
+    }
+  if (F) {
+    for (int k = 0; k < 3; ++k)
+      DPM_CUDA_TRY(cudaMemcpyAsync(soa.data() + k * V, b->d_f[k], sizeof(float) * V,
+                                   cudaMemcpyDeviceToHost, s));
+    DPM_CUDA_TRY(cudaStreamSynchronize(s));
+    for (long i = 0; i < V; ++i) {
+      F[3 * i] = soa[i];
+      F[3 * i + 1] = soa[V + i];
+      F[3 * i + 2] = soa[2 * V + i];
+    }
+  }
+  if (err & 1) return fail(DPM_ENONFINITE, "non-finite vertex positions");
+  return DPM_OK;
+}
+
+int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts) {
+  if (int r = check3(b)) return r;
+  if (!counts) return fail(DPM_EINVAL, "null output");
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(counts, b->d_wn, b->nverts, cudaMemcpyDeviceToHost,
+                               b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return DPM_OK;
+}
+
+int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel) {
+  if (int r = check3(b)) return r;
+  if (rebuild_period > 0) b->rebuild_period = rebuild_period;
+  if (skin_rel > 0.0f) b->skin_rel = skin_rel;
+  b->clear_graphs();
+  if (b->cells_set) {
+    b->update_skin();
+    if (b->tissues_set) {
+      cudaSetDevice(b->ctx->device);
+      DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
+                                   sizeof(Tissue3D) * b->ntissues, cudaMemcpyHostToDevice,
+                                   b->ctx->stream));
+      DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+    }
+  }
+  return DPM_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,125 @@
+"""3D parity of the CUDA path against the oracle, through the C ABI.
+
+Tolerances (FP32):
+  * forces of one step from the same positions: ||F - F_ref|| <= 1e-5 ||F_ref||
+  * positions after N steps: max |x - x_ref| / max(|x_ref|, 1) <= 1e-4
+  * winding-number hit counts: equal, except where the oracle's own sum sits
+    at the reference's 1e-6 threshold by rounding noise (at most 0.2% of
+    vertices may differ; their force contribution is ~1e-6 * Kc).
+"""
+import numpy as np
+import pytest
+
+from cases import gpu_batch3d, make_tissue3d, port, rel_norm_err
+
+pytestmark = pytest.mark.gpu
+
+DT = 0.005
+F_TOL = 1e-5
+X_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from opencl_dpm_gb300.abi import Context
+    return Context(0)
+
+
+def oracle_run(state, nsteps, dt=DT):
+    s = state.copy()
+    F, wn = port().run3d(s, nsteps, dt)
+    return s.xyz, F, wn
+
+
+def pos_err(x, ref):
+    return float(np.max(np.abs(x - ref) / np.maximum(np.abs(ref), 1.0)))
+
+
+def run_case(ctx, state, nsteps, tuning=None):
+    b = gpu_batch3d(ctx, [state], tuning)
+    b.step(nsteps, DT)
+    x, F = b.download()
+    wn = b.winding()
+    rx, rF, rwn = oracle_run(state, nsteps)
+    return x, F, wn, rx, rF, rwn
+
+
+def wn_mismatch(a, b):
+    return float(np.mean(a != b))
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_one_step_level2(ctx, seed):
+    s = make_tissue3d(6, level=2, phi0=0.5, seed=seed)
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 1)
+    assert rwn.sum() > 0  # the cells overlap: repulsion is exercised
+    assert wn_mismatch(wn, rwn) <= 2e-3
+    assert rel_norm_err(F, rF) <= F_TOL
+    assert pos_err(x, rx) <= X_TOL
+
+
+def test_50_steps_level2(ctx):
+    s = make_tissue3d(6, level=2, phi0=0.45, seed=3)
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 50)
+    assert pos_err(x, rx) <= X_TOL
+    # forces of one step from the GPU's positions
+    s2 = s.copy()
+    s2.xyz = x.copy()
+    b = gpu_batch3d(ctx, [s2])
+    b.step(1, DT)
+    _, F1 = b.download()
+    _, rF1, _ = oracle_run(s2, 1)
+    assert rel_norm_err(F1, rF1) <= F_TOL
+
+
+def test_level3(ctx):
+    s = make_tissue3d(4, level=3, phi0=0.5, seed=4)
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 1)
+    assert rel_norm_err(F, rF) <= F_TOL
+    assert wn_mismatch(wn, rwn) <= 2e-3
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 10)
+    assert pos_err(x, rx) <= X_TOL
+
+
+def test_bending_and_adhesion_range(ctx):
+    s = make_tissue3d(4, level=2, phi0=0.5, seed=5, Kb=0.05, adh=0.1)
+    # squash the meshes a little so that bending is active
+    s.xyz[:, 2] *= np.float32(0.9)
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 1)
+    assert rel_norm_err(F, rF) <= F_TOL
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 20)
+    assert pos_err(x, rx) <= X_TOL
+
+
+def test_no_repulsion_and_open_box(ctx):
+    s = make_tissue3d(5, level=2, phi0=0.5, seed=6, Kre=0.0, pbc=0)
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 5)
+    assert rel_norm_err(F, rF) <= F_TOL
+    assert wn.sum() == 0
+
+
+def test_batched_equals_alone_3d(ctx):
+    states = [make_tissue3d(int(n), level=2, phi0=0.5, seed=10 + n) for n in (3, 5, 4)]
+    b = gpu_batch3d(ctx, states)
+    b.step(12, DT)
+    x, F = b.download()
+    off = 0
+    for s in states:
+        n = s.ncells * s.nv
+        a = gpu_batch3d(ctx, [s])
+        a.step(12, DT)
+        ax, aF = a.download()
+        assert np.array_equal(ax, x[off:off + n])
+        rx, rF, _ = oracle_run(s, 12)
+        assert pos_err(x[off:off + n], rx) <= X_TOL
+        off += n
+
+
+def test_deterministic_3d(ctx):
+    s = make_tissue3d(6, level=2, phi0=0.5, seed=7)
+    out = []
+    for _ in range(2):
+        b = gpu_batch3d(ctx, [s])
+        b.step(10, DT)
+        out.append(b.download())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
