@@ -1,0 +1,429 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 DPM step (one JSON line on stdout).
+
+Workload (default, the batched 2D sweep): 512 independent tissues with
+N ~ U{8..256} cells and NV ~ {16, 24, 32, 48} vertices per cell (one NV per
+tissue), per-tissue kb ~ LogU[1e-3, 1e-1], calA0 ~ U[1.0, 1.3], true packing
+fraction ~ U[0.6, 0.9] (phi0 = sqrt(phi)), ka = kl = kc = 1, r0 = 1,
+dt = 0.005.  Cells start as the Cell2D constructor's regular polygons, centred
+on a seeded, jittered square lattice of the tissue's periodic box (synthetic
+data; the reference names no dataset).  All tissues step together in one
+batch; each simulation step is one launch of the fused step kernel, and the
+neighbour-list rebuild plus 16 steps are one captured CUDA graph.
+
+One benchmark "step" is one replay: 16 simulation steps of the whole batch.
+L2 (129 MB) is flushed by writing 256 MB before every timed iteration,
+outside the timed events.  value = vertices * simulation steps / time.
+
+Also reported: the plain single-tissue path on 1,024 bidisperse cells
+("plain"), the dominant kernel's roofline, the end-to-end rate through the C
+ABI with pinned host buffers ("e2e"), SM clocks during the timed region and
+the CPU baseline (the oracle restatement of the reference on the host cores).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "vertex-steps/s batched+served vs plain on 1 GB300; p50/p99 run latency; HBM GB/s"
+UNIT = "vertex-steps/s"
+DT = 0.005
+SIM_STEPS = 16
+L2_FLUSH_BYTES = 256 << 20
+
+
+# ---------------------------------------------------------------------------
+# workloads (built with the product's own host model, clDPM)
+# ---------------------------------------------------------------------------
+
+def lattice_centres(rng, n, L, jitter=0.1):
+    m = int(math.ceil(math.sqrt(n)))
+    sp = L / m
+    sites = rng.permutation(m * m)[:n]
+    ix, iy = sites % m, sites // m
+    c = np.stack([(ix + 0.5) * sp, (iy + 0.5) * sp], axis=1)
+    c += rng.uniform(-jitter * sp, jitter * sp, size=c.shape)
+    return c.astype(np.float32)
+
+
+def build_tissue(clDPM, rng, n, nv, calA, r0, Kb, phi):
+    """One tissue: regular polygons at lattice centres; returns arrays."""
+    proto = [clDPM.Cell2D(0.0, 0.0, float(calA[i]), int(nv[i]), float(r0[i])) for i in range(n)]
+    T = clDPM.Tissue2D(proto, float(np.sqrt(phi)))
+    L = T.L
+    cen = lattice_centres(rng, n, L)
+    xy, a0, l0 = [], [], []
+    for i, p in enumerate(proto):
+        v = np.asarray(p.Verts, np.float32) + cen[i]
+        xy.append(v)
+        a0.append(p.a0)
+        l0.append(p.l0)
+    return dict(nv=np.asarray(nv, np.uint32), xy=np.concatenate(xy), a0=np.float32(a0),
+                l0=np.float32(l0), r0=np.asarray(r0, np.float32),
+                Ka=np.ones(n, np.float32), Kl=np.ones(n, np.float32),
+                Kb=np.full(n, Kb, np.float32), L=np.float32(L), Kre=1.0, Kat=0.0)
+
+
+def workload_batched(seed=0, ntissues=512):
+    from opencl_dpm_gb300 import clDPM
+    rng = np.random.default_rng(seed)
+    tissues = []
+    for t in range(ntissues):
+        n = int(rng.integers(8, 257))
+        nv = int(rng.choice([16, 24, 32, 48]))
+        kb = float(10 ** rng.uniform(-3, -1))
+        calA = rng.uniform(1.0, 1.3, n)
+        phi = float(rng.uniform(0.6, 0.9))
+        tissues.append(build_tissue(clDPM, rng, n, np.full(n, nv), calA, np.ones(n), kb, phi))
+    return tissues
+
+
+def workload_plain(seed=1, n=1024):
+    from opencl_dpm_gb300 import clDPM
+    rng = np.random.default_rng(seed)
+    r0 = rng.permutation(np.r_[np.full(n // 2, 1.0), np.full(n - n // 2, 1.4)])
+    calA = rng.uniform(1.0, 1.2, n)
+    return [build_tissue(clDPM, rng, n, np.full(n, 32), calA, r0, 0.01, 0.6)]
+
+
+def make_batch(ctx, tissues):
+    from opencl_dpm_gb300.abi import Batch2D
+    cat = lambda k: np.concatenate([t[k] for t in tissues])
+    b = Batch2D(ctx, [len(t["nv"]) for t in tissues], cat("nv"))
+    b.set_cells(cat("Ka"), cat("Kl"), cat("Kb"), cat("a0"), cat("l0"), cat("r0"))
+    b.set_tissues([t["L"] for t in tissues], [t["Kre"] for t in tissues],
+                  [t["Kat"] for t in tissues], 1)
+    xy = cat("xy")
+    b.upload(xy)
+    return b, xy
+
+
+# ---------------------------------------------------------------------------
+# measurement helpers
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during timing."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            v = json.load(f)["hbm_gbs"]
+        return float(v), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def launches_per_block(batch, sim_steps):
+    lb, _, _, _ = batch.bins()
+    tbits = int(math.ceil(math.log2(batch.ntissues))) if batch.ntissues > 1 else 0
+    passes = (lb + tbits + 7) // 8
+    blocks = math.ceil(sim_steps / SIM_STEPS)
+    return blocks * (1 + 3 * passes + 1) + sim_steps
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from opencl_dpm_gb300.abi import Context
+
+    torch.cuda.set_device(local_rank)
+    ctx = Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local_rank)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+
+    tissues = workload_batched(seed=1000 + rank)
+    b, xy_host = make_batch(ctx, tissues)
+    V, N = b.nverts, b.ncells
+
+    def timed(batch, iters, fn):
+        total = 0.0
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(iters)]
+        with torch.cuda.stream(stream):
+            for i in range(iters):
+                flush.zero_()
+                ev[i][0].record(stream)
+                fn()
+                ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        for s, e in ev:
+            total += s.elapsed_time(e)
+        return total / 1e3
+
+    for _ in range(max(3, args.warmup)):
+        b.step(SIM_STEPS, DT)
+    ctx.synchronize()
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    secs = timed(b, args.steps, lambda: b.step(SIM_STEPS, DT))
+    clock_info = clocks.stop()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([secs], device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = float(t.item())
+        dist.barrier()
+    value = V * SIM_STEPS * args.steps * world / secs
+    ms_per_step = secs / args.steps * 1e3
+
+    if rank != 0:
+        return None
+
+    # dominant kernel: the fused step, launched alone after a flush
+    nk = 20
+    kern = timed(b, nk, lambda: b.step_kernel(DT)) / nk
+    bytes_per_launch = 16.0 * V + 28.0 * N
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_per_launch / kern / 1e9
+    traffic = profiled_traffic("k2d_step_batched")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS)",
+                "kernel": "k2d_step", "kernel_us": round(kern * 1e6, 2),
+                "bytes_per_launch": int(bytes_per_launch),
+                "traffic": None if traffic is None else int(traffic)}
+
+    # end to end through the C ABI: pinned host in, stepped, pinned host out
+    xy_pin = torch.from_numpy(np.ascontiguousarray(xy_host)).pin_memory()
+    out_pin = torch.empty_like(xy_pin).pin_memory()
+    f_pin = torch.empty_like(xy_pin).pin_memory()
+    e_iters = max(3, min(args.steps, 10))
+
+    def e2e_once():
+        b.upload_ptr(xy_pin.data_ptr())
+        b.step(SIM_STEPS, DT)
+        b.download_ptr(out_pin.data_ptr(), f_pin.data_ptr())
+
+    e2e_once()
+    # host wall time of the three calls (upload and download return only
+    # after their copies complete), L2 flushed before each iteration
+    tt = 0.0
+    for _ in range(e_iters):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e2e_once()
+        tt += time.perf_counter() - t1
+    e2e = {"value": round(V * SIM_STEPS * e_iters / tt, 1), "unit": UNIT,
+           "h2d_bytes_per_step": int(8 * V), "d2h_bytes_per_step": int(16 * V),
+           "path": "dpm2d_upload + dpm2d_step(16) + dpm2d_download, pinned host buffers"}
+
+    # plain single-tissue path (1,024 cells) for the batched/plain ratio
+    pt = workload_plain()
+    pb, _ = make_batch(ctx, pt)
+    for _ in range(3):
+        pb.step(SIM_STEPS, DT)
+    p_secs = timed(pb, max(3, args.steps), lambda: pb.step(SIM_STEPS, DT))
+    plain = {"value": round(pb.nverts * SIM_STEPS * max(3, args.steps) / p_secs, 1),
+             "unit": UNIT, "ms_per_step": round(p_secs / max(3, args.steps) * 1e3, 4),
+             "workload": "1 tissue, 1024 cells x 32 vertices, bidisperse r0 1.0/1.4, "
+                         "calA0 ~ U[1.0,1.2], kb=0.01, packing fraction 0.6 (static box)"}
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded tissues; see config)",
+        "config": {"workload": "batched 2D sweep: 512 tissues, N~U{8..256}, NV in {16,24,32,48}, "
+                               "kb~LogU[1e-3,1e-1], calA0~U[1,1.3], phi~U[0.6,0.9], "
+                               "ka=kl=kc=1, r0=1, dt=0.005",
+                   "tissues": b.ntissues, "cells": N, "vertices": V,
+                   "sim_steps_per_step": SIM_STEPS,
+                   "l2": "256 MB written before every timed iteration (outside the events)",
+                   "graph": "rebuild + 16 fused step launches per CUDA graph replay"},
+        "gpu_launches": launches_per_block(b, SIM_STEPS) * args.steps,
+        "roofline": roofline, "e2e": e2e, "plain": plain,
+        "batched_over_plain": round(value / world / plain["value"], 2),
+        "clocks": clock_info,
+    }
+    line["cpu_baseline"] = cpu_baseline(tissues, budget_s=args.cpu_budget)
+    return line
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline and the reference arm (the oracle; test/baseline use only)
+# ---------------------------------------------------------------------------
+
+def oracle_states(tissues):
+    from oracle.oracle import Tissue2DState
+    return [Tissue2DState(nv=t["nv"], xy=t["xy"].copy(), Ka=t["Ka"], Kl=t["Kl"], Kb=t["Kb"],
+                          a0=t["a0"], l0=t["l0"], r0=t["r0"], L=float(t["L"]), Kre=1.0, Kat=0.0)
+            for t in tissues]
+
+
+def cpu_sample(tissues, every=16):
+    return tissues[::every]
+
+
+def cpu_baseline(tissues, budget_s=10.0, steps=None):
+    from oracle.oracle import Port
+    P = Port()
+    sample = oracle_states(cpu_sample(tissues))
+    cores = os.cpu_count() or 1
+    verts = sum(int(s.nv.sum()) for s in sample)
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        for s in sample:
+            P.run2d(s, 1, DT, nthreads=cores)
+        done += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and done >= steps) or (steps is None and el >= budget_s):
+            break
+    return {"value": round(verts * done / el, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(sample)} of {len(tissues)} tissues (every 16th, {verts} vertices), "
+                      f"{done} steps, all-pairs reference algorithm, OpenMP over cells"}
+
+
+def run_reference(args):
+    tissues = workload_batched(seed=1000)
+    from oracle.oracle import Port
+    P = Port()
+    sample = oracle_states(cpu_sample(tissues))
+    cores = os.cpu_count() or 1
+    verts = sum(int(s.nv.sum()) for s in sample)
+    for _ in range(args.warmup):
+        for s in sample:
+            P.run2d(s, 1, DT, nthreads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in sample:
+            P.run2d(s, 1, DT, nthreads=cores)
+    secs = time.perf_counter() - t0
+    value = verts * args.steps / secs
+    desc = (f"{len(sample)} of {len(tissues)} tissues (every 16th, {verts} vertices), "
+            f"one simulation step per benchmark step, all-pairs reference algorithm")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded tissues)",
+            "config": {"workload": "batched 2D sweep (CPU sample)", "sample": desc},
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores,
+                             "kind": "port", "sample": desc},
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)), flush=True)
+        return 0
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    line = run_ours(args, rank, world, local_rank)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

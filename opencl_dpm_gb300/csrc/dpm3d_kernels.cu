@@ -69,10 +69,22 @@ __device__ float block_max(float v, float *red) {
   return r;
 }
 
-// Centre of mass (sum times 1/NV, Cell3D_Kernel.cl:35-44) and bounding
-// radius of the mesh held in shared memory.
+// Centre of mass (sum times 1/NV, Cell3D_Kernel.cl:35-44), bounding radius
+// and longest edge of the mesh held in shared memory.
+template <typename FaceIdx>
 __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, int nv,
-                            float *red) {
+                            const FaceIdx *faces, int nf, float *red) {
+  float e2 = 0.f;
+  for (int f = threadIdx.x; f < nf; f += kThreads) {
+    const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+    const int a[3] = {i0, i1, i2}, b[3] = {i1, i2, i0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float dx = px[a[k]] - px[b[k]], dy = py[a[k]] - py[b[k]], dz = pz[a[k]] - pz[b[k]];
+      e2 = fmaxf(e2, dx * dx + dy * dy + dz * dz);
+    }
+  }
+  const float emax = sqrtf(block_max(e2, red));
   float sx = 0.f, sy = 0.f, sz = 0.f;
   for (int v = threadIdx.x; v < nv; v += kThreads) {
     sx += px[v];
@@ -90,7 +102,20 @@ __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, i
     r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
   }
   g.R = sqrtf(block_max(r2, red));
+  g.emax = emax;
+  g.pad0 = g.pad1 = g.pad2 = 0.0f;
   return g;
+}
+
+// Radius around a cell's centre beyond which the reference's winding number
+// of a point is certainly below its 1e-6 threshold: outside the bounding
+// sphere every face lies farther than the point's distance to the sphere,
+// a face subtends more than pi steradians (denominator <= 0, dropped by the
+// reference) only from within 1.155 * its circumradius <= 0.77 * its
+// longest edge, and with no face dropped the sum over the closed mesh
+// cancels to rounding noise.
+__device__ __forceinline__ float winding_reach(const Geom3D &g) {
+  return g.R + 1.05f * g.emax;
 }
 
 // Shared-memory layout of k3d_step (see step3d_smem_bytes).
@@ -303,11 +328,12 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
       const f3 dc = C - cj;
       const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
                         fabsf(C.z);
-      const float rr = gi.R + gj.R + 1e-4f * (gi.R + gj.R) + 1e-5f * mag;
+      const float reach = winding_reach(gj);
+      const float rr = gi.R + reach + 1e-4f * (gi.R + reach) + 1e-5f * mag;
       if (!(dot(dc, dc) <= rr * rr)) continue;
       if (tid == 0) *s.ncand = 0;
       __syncthreads();
-      const float rj = gj.R * (1.0f + 1e-4f) + 1e-5f * mag;
+      const float rj = reach * (1.0f + 1e-4f) + 1e-5f * mag;
       for (int v = tid; v < NV; v += kThreads) {
         const f3 d = vtx(s, v) - cj;
         if (dot(d, d) <= rj * rj) s.cand[atomicAdd(s.ncand, 1)] = (uint16_t)v;
@@ -378,20 +404,24 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
     s.pz[v] = nz;
   }
   __syncthreads();
-  const Geom3D g = mesh_geom(s.px, s.py, s.pz, NV, s.red);
+  const Geom3D g = mesh_geom(s.px, s.py, s.pz, NV, s.faces, NF, s.red);
   if (tid == 0) {
     a.geom_out[c] = g;
     if (!(isfinite(g.cx) && isfinite(g.cy) && isfinite(g.cz) && isfinite(g.R)))
       atomicOr(a.err, 1);
+    // the list stays valid while every cell's winding reach moved by at
+    // most skin/2 (centre shift plus growth of R + 1.05 emax)
     const Geom3D g0 = a.geom0[c];
     const float dx = g.cx - g0.cx, dy = g.cy - g0.cy, dz = g.cz - g0.cz;
-    const float d = sqrtf(dx * dx + dy * dy + dz * dz) + fmaxf(0.0f, g.R - g0.R);
+    const float d = sqrtf(dx * dx + dy * dy + dz * dz) +
+                    fmaxf(0.0f, winding_reach(g) - winding_reach(g0)) + fmaxf(0.0f, g.R - g0.R);
     if (!(d <= 0.5f * T.skin)) atomicOr(a.stale + P.tissue, 1);
   }
 }
 
 __global__ void __launch_bounds__(kThreads)
-    k3d_geom(const float *x, const float *y, const float *z, Geom3D *geom, int nv) {
+    k3d_geom(const float *x, const float *y, const float *z, const uint16_t *faces, int nf,
+             Geom3D *geom, int nv) {
   __shared__ float px[kMaxNV3D], py[kMaxNV3D], pz[kMaxNV3D], red[64];
   const size_t base = (size_t)blockIdx.x * nv;
   for (int v = threadIdx.x; v < nv; v += kThreads) {
@@ -400,7 +430,7 @@ __global__ void __launch_bounds__(kThreads)
     pz[v] = z[base + v];
   }
   __syncthreads();
-  const Geom3D g = mesh_geom(px, py, pz, nv, red);
+  const Geom3D g = mesh_geom(px, py, pz, nv, faces, nf, red);
   if (threadIdx.x == 0) geom[blockIdx.x] = g;
 }
 
@@ -420,7 +450,7 @@ __global__ void __launch_bounds__(256) k3d_binprep(Rebuild3DArgs a, int local_bi
   const Tissue3D T = a.tissues[t];
   float dmax = 0.0f;
   for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x)
-    dmax = fmaxf(dmax, 2.0f * a.geom[c].R);
+    dmax = fmaxf(dmax, 2.0f * winding_reach(a.geom[c]));
   dmax = warp_max(dmax);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmax;
@@ -465,8 +495,12 @@ __device__ __forceinline__ bool pair3(const Geom3D &gi, const Geom3D &gj, const 
     dz = __fsub_rn(dz, __fmul_rn(T.L, roundf(__fdiv_rn(dz, T.L))));
   }
   const float mag = __fadd_rn(__fadd_rn(__fadd_rn(fabsf(gi.cx), fabsf(gi.cy)), fabsf(gi.cz)), T.L);
-  const float m = __fadd_rn(__fmul_rn(1e-3f, __fadd_rn(gi.R, gj.R)), __fmul_rn(1e-4f, mag));
-  const float r = __fadd_rn(__fadd_rn(__fadd_rn(gi.R, gj.R), T.skin), m);
+  // vertices of i (within R_i) that can reach j (within its winding reach),
+  // or the other way round
+  const float ri = winding_reach(gi), rj = winding_reach(gj);
+  const float span = fmaxf(__fadd_rn(gi.R, rj), __fadd_rn(gj.R, ri));
+  const float m = __fadd_rn(__fmul_rn(1e-3f, span), __fmul_rn(1e-4f, mag));
+  const float r = __fadd_rn(__fadd_rn(span, T.skin), m);
   const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
   return d2 <= __fmul_rn(r, r);
 }
@@ -557,9 +591,9 @@ cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_geom3d(const float *x, const float *y, const float *z, Geom3D *geom,
-                          int ncells, int nv, cudaStream_t s) {
-  k3d_geom<<<ncells, kThreads, 0, s>>>(x, y, z, geom, nv);
+cudaError_t launch_geom3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
+                          Geom3D *geom, int ncells, cudaStream_t s) {
+  k3d_geom<<<ncells, kThreads, 0, s>>>(x, y, z, mesh.faces, mesh.nf, geom, mesh.nv);
   return cudaGetLastError();
 }
 

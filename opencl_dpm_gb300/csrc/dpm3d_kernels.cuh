@@ -44,8 +44,8 @@ struct Rebuild3DArgs {
   int ncells, ntissues;
 };
 
-cudaError_t launch_geom3d(const float *x, const float *y, const float *z, Geom3D *geom,
-                          int ncells, int nv, cudaStream_t s);
+cudaError_t launch_geom3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
+                          Geom3D *geom, int ncells, cudaStream_t s);
 cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 size_t step3d_smem_bytes(int nv, int nf, bool bend);

@@ -78,9 +78,13 @@ struct alignas(16) Tissue3D {
   int pbc, cell_begin, cell_end, cap;
   int nb, pad0, pad1, pad2;
 };
-// Centre of mass and largest vertex distance from it.
+// Centre of mass, largest vertex distance from it, and the longest mesh
+// edge (the reference's winding sum drops faces whose denominator is below
+// 1e-8, which happens only within ~0.77 * longest edge of a face, so points
+// up to R + emax from the centre can get a non-zero winding number).
 struct alignas(16) Geom3D {
   float cx, cy, cz, R;
+  float emax, pad0, pad1, pad2;
 };
 constexpr int kMaxNB3D = 64;
 

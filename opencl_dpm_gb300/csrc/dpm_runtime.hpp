@@ -5,15 +5,23 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <atomic>
+
+// A context is shared by the objects created from it: each holds a
+// reference, so destroying the context (or the objects) in any order is
+// safe; the stream is released with the last reference.
 struct dpm_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int sm_count = 0;
+  std::atomic<int> refs{1};
 };
 
 namespace dpm {
 
 const char *last_error();
+void ctx_retain(dpm_ctx *ctx);
+void ctx_release(dpm_ctx *ctx);
 
 // One device allocation carved into 256-byte aligned arrays.  A batch owns
 // its arena; nothing else allocates on the step path.

@@ -43,6 +43,16 @@ int cuda_fail(cudaError_t e, const char *what) {
 }
 const char *last_error() { return g_last_error.c_str(); }
 
+void ctx_retain(dpm_ctx *ctx) { ctx->refs.fetch_add(1); }
+
+void ctx_release(dpm_ctx *ctx) {
+  if (ctx->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
 static int ceil_log2(long v) {
   int b = 0;
   while ((1L << b) < v) ++b;
@@ -224,10 +234,7 @@ int dpm_ctx_create(int device, dpm_ctx **out) {
 
 int dpm_ctx_destroy(dpm_ctx *ctx) {
   if (!ctx) return DPM_OK;
-  cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
-  cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  dpm::ctx_release(ctx);
   return DPM_OK;
 }
 
@@ -329,6 +336,7 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     e = cudaMemsetAsync(A.base(), 0, A.used(), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
     *out = b.release();
+    ctx_retain(ctx);
     return DPM_OK;
   } catch (const std::bad_alloc &) {
     return fail(DPM_ECAPACITY, "out of host memory");
@@ -339,7 +347,9 @@ int dpm2d_destroy(dpm2d_batch *b) {
   if (!b) return DPM_OK;
   cudaSetDevice(b->ctx->device);
   cudaStreamSynchronize(b->ctx->stream);
+  dpm_ctx *c = b->ctx;
   delete b;
+  ctx_release(c);
   return DPM_OK;
 }
 

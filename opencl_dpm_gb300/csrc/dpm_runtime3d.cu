@@ -305,6 +305,7 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
     e = prepare_step3d(nv, nf, true);
     if (e != cudaSuccess) return cuda_fail(e, "shared-memory opt-in");
     *out = b.release();
+    ctx_retain(ctx);
     return DPM_OK;
   } catch (const std::bad_alloc &) {
     return fail(DPM_ECAPACITY, "out of host memory");
@@ -315,7 +316,9 @@ int dpm3d_destroy(dpm3d_batch *b) {
   if (!b) return DPM_OK;
   cudaSetDevice(b->ctx->device);
   cudaStreamSynchronize(b->ctx->stream);
+  dpm_ctx *c = b->ctx;
   delete b;
+  ctx_release(c);
   return DPM_OK;
 }
 
@@ -413,8 +416,8 @@ int dpm3d_upload(dpm3d_batch *b, const float *xyz) {
   for (int k = 0; k < 3; ++k) DPM_CUDA_TRY(cudaMemsetAsync(b->d_f[k], 0, sizeof(float) * V, s));
   DPM_CUDA_TRY(cudaMemsetAsync(b->d_wn, 0, V, s));
   DPM_CUDA_TRY(cudaMemsetAsync(b->d_err, 0, sizeof(int), s));
-  DPM_CUDA_TRY(launch_geom3d(b->d_pos[0][0], b->d_pos[0][1], b->d_pos[0][2], b->d_geom[0],
-                             b->ncells, b->nv, s));
+  DPM_CUDA_TRY(launch_geom3d(b->d_pos[0][0], b->d_pos[0][1], b->d_pos[0][2], b->mesh,
+                             b->d_geom[0], b->ncells, s));
   DPM_CUDA_TRY(cudaStreamSynchronize(s));
   b->uploaded = true;
   return DPM_OK;
