@@ -9,9 +9,12 @@ dt = 0.005.  Cells start as the Cell2D constructor's regular polygons, centred
 on a seeded, jittered square lattice of the tissue's periodic box (synthetic
 data; the reference names no dataset).  All tissues step together in one
 batch; each simulation step is one launch of the fused step kernel, and the
-neighbour-list rebuild plus 16 steps are one captured CUDA graph.
+neighbour-list rebuild plus one rebuild period of steps (8, 16 or 32, chosen
+with warps per block and the register variant by the project's autotuner,
+dpm2d_autotune) are one captured CUDA graph.
 
-One benchmark "step" is one replay: 16 simulation steps of the whole batch.
+One benchmark "step" is one dpm2d_step call of 32 simulation steps of the
+whole batch.
 L2 (129 MB) is flushed by writing 256 MB before every timed iteration,
 outside the timed events.  value = vertices * simulation steps / time.
 
@@ -41,7 +44,7 @@ sys.path.insert(0, ROOT)
 METRIC = "vertex-steps/s batched+served vs plain on 1 GB300; p50/p99 run latency; HBM GB/s"
 UNIT = "vertex-steps/s"
 DT = 0.005
-SIM_STEPS = 16
+SIM_STEPS = 32  # simulation steps per benchmark step (a multiple of every rebuild period)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -191,11 +194,14 @@ def profiled_traffic(kernel):
         return None
 
 
-def launches_per_block(batch, sim_steps):
+def launches_per_call(batch, sim_steps, period):
+    """Kernel launches of one dpm2d_step(sim_steps): per rebuild period one
+    bin-preparation launch, 3 launches per radix pass, one neighbour-list
+    launch; one fused step launch per simulation step."""
     lb, _, _, _ = batch.bins()
     tbits = int(math.ceil(math.log2(batch.ntissues))) if batch.ntissues > 1 else 0
     passes = (lb + tbits + 7) // 8
-    blocks = math.ceil(sim_steps / SIM_STEPS)
+    blocks = math.ceil(sim_steps / period)
     return blocks * (1 + 3 * passes + 1) + sim_steps
 
 
@@ -215,6 +221,7 @@ def run_ours(args, rank, world, local_rank):
     tissues = workload_batched(seed=1000 + rank)
     b, xy_host = make_batch(ctx, tissues)
     V, N = b.nverts, b.ncells
+    tuned = b.autotune(DT, trial_blocks=2, use_cache=True)
 
     def timed(batch, iters, fn):
         total = 0.0
@@ -293,18 +300,20 @@ def run_ours(args, rank, world, local_rank):
         tt += time.perf_counter() - t1
     e2e = {"value": round(V * SIM_STEPS * e_iters / tt, 1), "unit": UNIT,
            "h2d_bytes_per_step": int(8 * V), "d2h_bytes_per_step": int(16 * V),
-           "path": "dpm2d_upload + dpm2d_step(16) + dpm2d_download, pinned host buffers"}
+           "path": "dpm2d_upload + dpm2d_step(32) + dpm2d_download, pinned host buffers"}
 
     # plain single-tissue path (1,024 cells) for the batched/plain ratio
     pt = workload_plain()
     pb, _ = make_batch(ctx, pt)
+    ptuned = pb.autotune(DT, trial_blocks=2, use_cache=True)
     for _ in range(3):
         pb.step(SIM_STEPS, DT)
     p_secs = timed(pb, max(3, args.steps), lambda: pb.step(SIM_STEPS, DT))
     plain = {"value": round(pb.nverts * SIM_STEPS * max(3, args.steps) / p_secs, 1),
              "unit": UNIT, "ms_per_step": round(p_secs / max(3, args.steps) * 1e3, 4),
              "workload": "1 tissue, 1024 cells x 32 vertices, bidisperse r0 1.0/1.4, "
-                         "calA0 ~ U[1.0,1.2], kb=0.01, packing fraction 0.6 (static box)"}
+                         "calA0 ~ U[1.0,1.2], kb=0.01, packing fraction 0.6 (static box)",
+             "tuning": ptuned}
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -317,8 +326,9 @@ def run_ours(args, rank, world, local_rank):
                    "tissues": b.ntissues, "cells": N, "vertices": V,
                    "sim_steps_per_step": SIM_STEPS,
                    "l2": "256 MB written before every timed iteration (outside the events)",
-                   "graph": "rebuild + 16 fused step launches per CUDA graph replay"},
-        "gpu_launches": launches_per_block(b, SIM_STEPS) * args.steps,
+                   "graph": "one CUDA graph replay per cell-list rebuild period",
+                   "tuning": tuned},
+        "gpu_launches": launches_per_call(b, SIM_STEPS, tuned["rebuild_period"]) * args.steps,
         "roofline": roofline, "e2e": e2e, "plain": plain,
         "batched_over_plain": round(value / world / plain["value"], 2),
         "clocks": clock_info,

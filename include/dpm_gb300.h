@@ -136,6 +136,18 @@ int dpm2d_bins(dpm2d_batch *b, int *local_bits, int *nbins, float *binw,
  * synchronizing.  For per-kernel timing and profiling. */
 int dpm2d_step_kernel(dpm2d_batch *b, float dt);
 
+/* Autotuner: times warps per block (4, 8, 16) x register/occupancy variant
+ * (0: compiler's choice, 1: 32 resident warps per SM) x (rebuild period,
+ * skin) on this batch's current state, restores the state, and applies the
+ * fastest.  Choices are cached as JSON lines keyed by the batch's shape in
+ * $DPM_TUNE_CACHE (default ~/.cache/dpm_gb300_tune2d.jsonl); with use_cache
+ * a cached choice is applied without trials.  Allocates a temporary copy of
+ * the state while tuning.  Outputs may be NULL; ms_per_step is -1 when the
+ * choice came from the cache. */
+int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache,
+                   int *warps, int *occupancy, int *rebuild_period,
+                   float *skin_rel, float *ms_per_step);
+
 /* ---------------------------------------------------------------------- */
 /* 3D batches                                                              */
 /* ---------------------------------------------------------------------- */

@@ -48,6 +48,8 @@ SIGNATURES = {
                                        _c_float_p]),
     "dpm2d_bins": (ctypes.c_int, [_vp, _c_int_p, _c_int_p, _c_float_p, _c_float_p]),
     "dpm2d_step_kernel": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "dpm2d_autotune": (ctypes.c_int, [_vp, ctypes.c_float, ctypes.c_int, ctypes.c_int, _c_int_p,
+                                      _c_int_p, _c_int_p, _c_float_p, _c_float_p]),
     "dpm3d_create": (ctypes.c_int, [_vp, ctypes.c_int, _c_int_p, ctypes.c_int, ctypes.c_int,
                                     _c_uint_p, ctypes.POINTER(_vp)]),
     "dpm3d_destroy": (ctypes.c_int, [_vp]),
@@ -213,6 +215,15 @@ class Batch2D:
 
     def step_kernel(self, dt: float):
         check(self.lib.dpm2d_step_kernel(self.h, dt))
+
+    def autotune(self, dt: float, trial_blocks: int = 2, use_cache: bool = True) -> dict:
+        w, o, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        sk, ms = ctypes.c_float(), ctypes.c_float()
+        check(self.lib.dpm2d_autotune(self.h, dt, trial_blocks, int(use_cache), ctypes.byref(w),
+                                      ctypes.byref(o), ctypes.byref(p), ctypes.byref(sk),
+                                      ctypes.byref(ms)))
+        return {"warps": w.value, "occupancy": o.value, "rebuild_period": p.value,
+                "skin_rel": round(sk.value, 4), "ms_per_step": round(ms.value, 5)}
 
     def rebuild_now(self):
         check(self.lib.dpm2d_rebuild_now(self.h))

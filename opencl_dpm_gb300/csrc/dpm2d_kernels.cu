@@ -94,22 +94,24 @@ __device__ __forceinline__ unsigned edge_crosses(float X, float Y, float pix, fl
 //    sign and the count equals the even-odd containment, which is 0.
 //  * A shift happens only if some vertex is more than L away on an axis;
 //    by monotone rounding that is decided exactly by the box corners.
+//  * If only x offsets can be shifted, the y test still compares the raw
+//    signs of Y - P.y, so again an odd count needs miny < Y <= maxy.
 __device__ __forceinline__ bool vertex_candidate(float X, float Y, const Geom2D &gj,
                                                  bool near, bool far, float L) {
-  if (near) {
+  const bool band = Y > gj.miny && Y <= gj.maxy;
+  if (far) {
+    const bool fy = __fsub_rn(Y, gj.miny) > L || __fsub_rn(gj.maxy, Y) > L;
+    if (fy) return true;
+    const bool fx = __fsub_rn(X, gj.minx) > L || __fsub_rn(gj.maxx, X) > L;
+    if (fx) return band;
+  }
+  if (near && band) {
     const float dx = X - gj.cx, dy = Y - gj.cy;
     const float rm = gj.R * (1.0f + kRelMargin) +
                      kAbsMargin * (fabsf(gj.cx) + fabsf(gj.cy) + fabsf(X) + fabsf(Y));
     const float bm = kRelMargin * (gj.maxx - gj.minx) +
                      kAbsMargin * (fabsf(gj.minx) + fabsf(gj.maxx) + fabsf(X));
-    if (Y > gj.miny && Y <= gj.maxy && X >= gj.minx - bm && X <= gj.maxx + bm &&
-        dx * dx + dy * dy <= rm * rm)
-      return true;
-  }
-  if (far) {
-    if (__fsub_rn(X, gj.minx) > L || __fsub_rn(gj.maxx, X) > L ||
-        __fsub_rn(Y, gj.miny) > L || __fsub_rn(gj.maxy, Y) > L)
-      return true;
+    if (X >= gj.minx - bm && X <= gj.maxx + bm && dx * dx + dy * dy <= rm * rm) return true;
   }
   return false;
 }
@@ -381,8 +383,18 @@ __global__ void __launch_bounds__(kNbWarps * 32) k2d_neighbors(Rebuild2DArgs a, 
 // Fused step
 // ---------------------------------------------------------------------------
 
-template <int S, int W>
-__global__ void __launch_bounds__(W * 32) k2d_step(Step2DArgs a) {
+// Occupancy variants: with OCC = 1 the register budget is capped so that
+// 32 warps per SM stay resident (16 for more than 2 vertex slots per lane);
+// with OCC = 0 the compiler chooses.  The tuner picks per batch.
+template <int S, int W, int OCC> struct StepOcc {
+  static constexpr int kThreads = S <= 2 ? 1024 : 512;
+  static constexpr int kBlocks =
+      OCC == 0 ? 1 : (kThreads / (W * 32) > 0 ? kThreads / (W * 32) : 1);
+};
+
+template <int S, int W, int OCC>
+__global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
+    k2d_step(Step2DArgs a) {
   constexpr int M = 32 * S;
   __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
   __shared__ unsigned char sh_f[W][M];
@@ -456,33 +468,67 @@ __global__ void __launch_bounds__(W * 32) k2d_step(Step2DArgs a) {
   const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
   const int *list = a.nbr + (size_t)c * kMaxNB2D;
   const bool att = T.Kat != 0.0f;
-  for (int q = 0; q < count; ++q) {
-    const int j = scan_all ? T.cell_begin + q : list[q];
-    if (j == c) continue;
-    const Geom2D gj = a.geom_in[j];
-    const float dcx = gi.cx - gj.cx, dcy = gi.cy - gj.cy;
-    const float rr = gi.R + gj.R;
-    const float mm = kRelMargin * rr +
-                     kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) + fabsf(gj.cx) + fabsf(gj.cy));
-    const bool near = dcx * dcx + dcy * dcy <= (rr + mm) * (rr + mm);
-    const bool far = pbc && (__fsub_rn(gi.maxx, gj.minx) > L || __fsub_rn(gj.maxx, gi.minx) > L ||
-                             __fsub_rn(gi.maxy, gj.miny) > L || __fsub_rn(gj.maxy, gi.miny) > L);
-    bool attp = false;
-    if (att) {
-      float ex = dcx, ey = dcy;
-      if (pbc) {
-        ex -= L * roundf(ex / L);
-        ey -= L * roundf(ey / L);
+  // Lanes screen up to 32 list entries at once (one geometry load each, in
+  // parallel); the cells that pass are then processed one by one, in list
+  // order, with their geometry broadcast by shuffles.
+  for (int base = 0; base < count; base += 32) {
+    const int q = base + lane;
+    int jl = -1;
+    unsigned pflags = 0u;
+    Geom2D gl;
+    gl.cx = gl.cy = gl.R = gl.area = gl.minx = gl.maxx = gl.miny = gl.maxy = 0.0f;
+    if (q < count) {
+      jl = scan_all ? T.cell_begin + q : list[q];
+      if (jl != c) {
+        gl = a.geom_in[jl];
+        const float dcx = gi.cx - gl.cx, dcy = gi.cy - gl.cy;
+        const float rr = gi.R + gl.R;
+        const float mm = kRelMargin * rr + kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) +
+                                                         fabsf(gl.cx) + fabsf(gl.cy));
+        // own y range must meet (miny_j, maxy_j] unless y offsets can shift
+        const bool yover = gi.maxy > gl.miny && gi.miny <= gl.maxy;
+        const bool near = yover && dcx * dcx + dcy * dcy <= (rr + mm) * (rr + mm);
+        const bool farx = pbc && (__fsub_rn(gi.maxx, gl.minx) > L || __fsub_rn(gl.maxx, gi.minx) > L);
+        const bool fary = pbc && (__fsub_rn(gi.maxy, gl.miny) > L || __fsub_rn(gl.maxy, gi.miny) > L);
+        const bool far = fary || (farx && yover);
+        bool attp = false;
+        if (att) {
+          float ex = dcx, ey = dcy;
+          if (pbc) {
+            ex -= L * roundf(ex / L);
+            ey -= L * roundf(ey / L);
+          }
+          const float ra = rr + cp.l0 + mm;
+          attp = ex * ex + ey * ey <= ra * ra;
+        }
+        pflags = (near ? 1u : 0u) | (far ? 2u : 0u) | (attp ? 4u : 0u);
       }
-      const float ra = rr + cp.l0 + mm;
-      attp = ex * ex + ey * ey <= ra * ra;
     }
-    if (!near && !far && !attp) continue;
+    unsigned pm = __ballot_sync(kFull, pflags != 0u);
+    while (pm) {
+    const int src = __ffs(pm) - 1;
+    pm &= pm - 1u;
+    const int j = __shfl_sync(kFull, jl, src);
+    const unsigned fl = __shfl_sync(kFull, pflags, src);
+    const bool near = fl & 1u, far = fl & 2u, attp = fl & 4u;
+    Geom2D gj;
+    gj.cx = __shfl_sync(kFull, gl.cx, src);
+    gj.cy = __shfl_sync(kFull, gl.cy, src);
+    gj.R = __shfl_sync(kFull, gl.R, src);
+    gj.area = 0.0f;
+    gj.minx = __shfl_sync(kFull, gl.minx, src);
+    gj.maxx = __shfl_sync(kFull, gl.maxx, src);
+    gj.miny = __shfl_sync(kFull, gl.miny, src);
+    gj.maxy = __shfl_sync(kFull, gl.maxy, src);
+    const float mm = kRelMargin * (gi.R + gj.R) +
+                     kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) + fabsf(gj.cx) + fabsf(gj.cy));
 
     unsigned cm[S], am[S];
     bool anyc = false, anya = false;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
+      cm[s] = am[s] = 0u;
+      if (32 * s >= n) continue;  // empty slot (uniform over the warp)
       const int k = lane + 32 * s;
       bool cand = false, ac = false;
       if (k < n) {
@@ -498,9 +544,11 @@ __global__ void __launch_bounds__(W * 32) k2d_step(Step2DArgs a) {
         }
       }
       cm[s] = __ballot_sync(kFull, cand);
-      am[s] = __ballot_sync(kFull, ac);
       anyc |= cm[s] != 0u;
-      anya |= am[s] != 0u;
+      if (att) {
+        am[s] = __ballot_sync(kFull, ac);
+        anya |= am[s] != 0u;
+      }
     }
     if (!anyc && !anya) continue;
 
@@ -560,6 +608,7 @@ __global__ void __launch_bounds__(W * 32) k2d_step(Step2DArgs a) {
       }
     }
     __syncwarp();
+    }
   }
 
   // -- repulsion force toward the own centre (Cell2D_kernel.cl:205-219)
@@ -612,19 +661,24 @@ __global__ void __launch_bounds__(W * 32) k2d_step(Step2DArgs a) {
   }
 }
 
-template <int S, int W>
+template <int S, int W, int OCC>
 cudaError_t launch_step_sw(const Step2DArgs &a, cudaStream_t s) {
   const int grid = (a.ncells + W - 1) / W;
-  k2d_step<S, W><<<grid, W * 32, 0, s>>>(a);
+  k2d_step<S, W, OCC><<<grid, W * 32, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-template <int S>
-cudaError_t launch_step_s(const Step2DArgs &a, int warps, cudaStream_t s) {
+template <int S, int OCC>
+cudaError_t launch_step_so(const Step2DArgs &a, int warps, cudaStream_t s) {
   // 16 warps of 8 slots would exceed the static shared-memory limit
-  if (warps == 4) return launch_step_sw<S, 4>(a, s);
-  if (warps == 16 && S <= 4) return launch_step_sw<S, (S <= 4 ? 16 : 8)>(a, s);
-  return launch_step_sw<S, 8>(a, s);
+  if (warps == 4) return launch_step_sw<S, 4, OCC>(a, s);
+  if (warps == 16 && S <= 4) return launch_step_sw<S, (S <= 4 ? 16 : 8), OCC>(a, s);
+  return launch_step_sw<S, 8, OCC>(a, s);
+}
+
+template <int S>
+cudaError_t launch_step_s(const Step2DArgs &a, int warps, int occ, cudaStream_t s) {
+  return occ ? launch_step_so<S, 1>(a, warps, s) : launch_step_so<S, 0>(a, warps, s);
 }
 
 } // namespace
@@ -653,11 +707,11 @@ cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStrea
   return cudaGetLastError();
 }
 
-cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, cudaStream_t s) {
-  if (maxnv <= 32) return launch_step_s<1>(a, warps, s);
-  if (maxnv <= 64) return launch_step_s<2>(a, warps, s);
-  if (maxnv <= 128) return launch_step_s<4>(a, warps, s);
-  return launch_step_s<8>(a, warps, s);
+cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int occ, cudaStream_t s) {
+  if (maxnv <= 32) return launch_step_s<1>(a, warps, occ, s);
+  if (maxnv <= 64) return launch_step_s<2>(a, warps, occ, s);
+  if (maxnv <= 128) return launch_step_s<4>(a, warps, occ, s);
+  return launch_step_s<8>(a, warps, occ, s);
 }
 
 } // namespace dpm

@@ -46,8 +46,9 @@ cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom,
 cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
 // Neighbour lists from the sorted cell list (one warp per cell).
 cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
-// One fused time step.
-cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps,
+// One fused time step.  warps: 4, 8 or 16 per block; occ: 1 caps registers
+// for 32 resident warps per SM, 0 lets the compiler choose.
+cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int occ,
                           cudaStream_t s);
 
 // Host mirror of the bin arithmetic (for the host rebuild check).

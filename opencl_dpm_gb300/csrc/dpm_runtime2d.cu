@@ -9,9 +9,12 @@
 // call.  Graphs are instantiated once per (block length, parity, dt, last)
 // and replayed.
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -92,6 +95,7 @@ struct dpm2d_batch {
   int rebuild_period = 16;
   float skin_rel = 0.15f;
   int warps = 8;
+  int occ = 1;
   long rebuilds = 0;
 
   std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
@@ -162,7 +166,7 @@ struct dpm2d_batch {
     if (e != cudaSuccess) return e;
     int f = from;
     for (int i = 0; i < len; ++i) {
-      e = launch_step2d(step_args(f, dt, last && i == len - 1), maxnv, warps, s);
+      e = launch_step2d(step_args(f, dt, last && i == len - 1), maxnv, warps, occ, s);
       if (e != cudaSuccess) return e;
       f = 1 - f;
     }
@@ -488,7 +492,8 @@ int dpm2d_step_kernel(dpm2d_batch *b, float dt) {
   if (int r = check_batch(b)) return r;
   if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before stepping");
   cudaSetDevice(b->ctx->device);
-  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true), b->maxnv, b->warps, b->ctx->stream));
+  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true), b->maxnv, b->warps, b->occ,
+                             b->ctx->stream));
   b->cur = 1 - b->cur;
   return DPM_OK;
 }
@@ -595,6 +600,177 @@ int dpm2d_cell_list(dpm2d_batch *b, unsigned *keys, unsigned *ids, int *nn, int 
                                  cudaMemcpyDeviceToHost, s));
   if (maxnb) *maxnb = kMaxNB2D;
   DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  return DPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: warps per block x occupancy variant x (rebuild period, skin)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+std::string tune_cache_path() {
+  if (const char *p = std::getenv("DPM_TUNE_CACHE")) return p;
+  const char *home = std::getenv("HOME");
+  return std::string(home ? home : ".") + "/.cache/dpm_gb300_tune2d.jsonl";
+}
+
+std::string tune_key(const dpm2d_batch *b, int sm_count) {
+  // shape buckets: the choice depends on work per launch, not on exact sizes
+  auto bucket = [](long v) {
+    int k = 0;
+    while ((1L << k) < v) ++k;
+    return k;
+  };
+  char buf[160];
+  std::snprintf(buf, sizeof(buf), "2d sm%d t%d c%d v%d nv%d", sm_count, bucket(b->ntissues),
+                bucket(b->ncells), bucket(b->nverts), b->maxnv);
+  return buf;
+}
+
+bool tune_lookup(const std::string &key, int *warps, int *occ, int *period, float *skin) {
+  FILE *f = std::fopen(tune_cache_path().c_str(), "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (std::fgets(line, sizeof(line), f)) {
+    char k[200];
+    int w, o, p;
+    float sk;
+    if (std::sscanf(line, "{\"key\": \"%199[^\"]\", \"warps\": %d, \"occ\": %d, \"period\": %d, "
+                          "\"skin_rel\": %f",
+                    k, &w, &o, &p, &sk) == 5 &&
+        key == k) {
+      *warps = w;
+      *occ = o;
+      *period = p;
+      *skin = sk;
+      found = true;  // the last entry for a key wins
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+void tune_store(const std::string &key, int warps, int occ, int period, float skin, float ms) {
+  const std::string path = tune_cache_path();
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos) {
+    const std::string dir = path.substr(0, slash);
+    for (size_t i = 1; i <= dir.size(); ++i)
+      if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
+  }
+  FILE *f = std::fopen(path.c_str(), "a");
+  if (!f) return;
+  std::fprintf(f,
+               "{\"key\": \"%s\", \"warps\": %d, \"occ\": %d, \"period\": %d, \"skin_rel\": %.4f, "
+               "\"ms_per_step\": %.5f}\n",
+               key.c_str(), warps, occ, period, skin, ms);
+  std::fclose(f);
+}
+
+} // namespace
+
+int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache, int *warps_out,
+                   int *occ_out, int *period_out, float *skin_out, float *ms_out) {
+  if (int r = check_batch(b)) return r;
+  if (!b->uploaded || !b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues and upload before tuning");
+  if (trial_blocks <= 0) trial_blocks = 2;
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->ctx->stream;
+  const std::string key = tune_key(b, b->ctx->sm_count);
+  int w = 0, o = 0, p = 0;
+  float sk = 0.0f, best_ms = -1.0f;
+  auto apply = [&](int ww, int oo, int pp, float ss) -> int {
+    b->warps = ww;
+    b->occ = oo;
+    b->rebuild_period = pp;
+    b->skin_rel = ss;
+    b->clear_graphs();
+    for (int t = 0; t < b->ntissues; ++t) {
+      Tissue2D &T = b->h_tissues[t];
+      double rsum = 0.0;
+      for (int c = T.cell_begin; c < T.cell_end; ++c) rsum += b->h_cells[c].r0;
+      T.skin = (float)(ss * 2.0 * rsum / (T.cell_end - T.cell_begin));
+    }
+    DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
+                                 sizeof(Tissue2D) * b->ntissues, cudaMemcpyHostToDevice, s));
+    return DPM_OK;
+  };
+  if (use_cache && tune_lookup(key, &w, &o, &p, &sk)) {
+    if (int r = apply(w, o, p, sk)) return r;
+  } else {
+    // save the state: the trials advance the simulation
+    const size_t pos_bytes = sizeof(float2) * b->nverts, geom_bytes = sizeof(Geom2D) * b->ncells;
+    void *save = nullptr;
+    DPM_CUDA_TRY(cudaMalloc(&save, pos_bytes + geom_bytes));
+    const int cur0 = b->cur;
+    DPM_CUDA_TRY(cudaMemcpyAsync(save, b->d_pos[cur0], pos_bytes, cudaMemcpyDeviceToDevice, s));
+    DPM_CUDA_TRY(cudaMemcpyAsync((char *)save + pos_bytes, b->d_geom[cur0], geom_bytes,
+                                 cudaMemcpyDeviceToDevice, s));
+    auto restore = [&]() -> cudaError_t {
+      b->cur = cur0;
+      cudaError_t e = cudaMemcpyAsync(b->d_pos[cur0], save, pos_bytes, cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_geom[cur0], (char *)save + pos_bytes, geom_bytes,
+                            cudaMemcpyDeviceToDevice, s);
+      return e;
+    };
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int warps_set[3] = {4, 8, 16};
+    const int periods[3] = {8, 16, 32};
+    const float skins[3] = {0.08f, 0.15f, 0.3f};
+    int rc = DPM_OK;
+    for (int wi = 0; wi < 3 && rc == DPM_OK; ++wi)
+      for (int oi = 0; oi < 2 && rc == DPM_OK; ++oi)
+        for (int pi = 0; pi < 3 && rc == DPM_OK; ++pi) {
+          if (warps_set[wi] == 16 && b->maxnv > 128) continue;
+          if ((rc = apply(warps_set[wi], oi, periods[pi], skins[pi]))) break;
+          cudaError_t e = restore();
+          if (e != cudaSuccess) {
+            rc = cuda_fail(e, "tuner restore");
+            break;
+          }
+          if ((rc = b->run_block(periods[pi], dt, false))) break;  // warm: capture
+          cudaEventRecord(e0, s);
+          for (int k = 0; k < trial_blocks && rc == DPM_OK; ++k)
+            rc = b->run_block(periods[pi], dt, false);
+          cudaEventRecord(e1, s);
+          e = cudaEventSynchronize(e1);
+          if (e != cudaSuccess) {
+            rc = cuda_fail(e, "tuner timing");
+            break;
+          }
+          float ms = 0.0f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          ms /= (float)(trial_blocks * periods[pi]);
+          if (best_ms < 0.0f || ms < best_ms) {
+            best_ms = ms;
+            w = warps_set[wi];
+            o = oi;
+            p = periods[pi];
+            sk = skins[pi];
+          }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t e = restore();
+    cudaStreamSynchronize(s);
+    cudaFree(save);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "tuner restore");
+    if (int r = apply(w, o, p, sk)) return r;
+    tune_store(key, w, o, p, sk, best_ms);
+  }
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (warps_out) *warps_out = w;
+  if (occ_out) *occ_out = o;
+  if (period_out) *period_out = p;
+  if (skin_out) *skin_out = sk;
+  if (ms_out) *ms_out = best_ms;
   return DPM_OK;
 }
 
