@@ -149,6 +149,38 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache,
                    float *skin_rel, float *ms_per_step);
 
 /* ---------------------------------------------------------------------- */
+/* 2D step without device allocation                                       */
+/* ---------------------------------------------------------------------- */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- a program whose device memory belongs to another framework's
+ * pool, code that must not synchronize the device the way cudaMalloc and
+ * cudaFree can, or an embedded use that reserves all memory at start-up.
+ *
+ * Runs nsteps steps of one 2D tissue, exactly as a one-tissue dpm2d batch
+ * does, and allocates nothing: the caller passes its own DEVICE buffer of
+ * positions (xy_dev, float[2*total], updated in place) and optionally one for
+ * the last step's forces (F_dev, may be NULL); the per-cell constants (nv,
+ * Ka, Kl, Kb, a0, l0, r0) are HOST arrays.  All other working memory is one
+ * fixed device array inside the library (about 1.7 MB, held on every GPU that
+ * loads the library until the process exits), so:
+ *   - ncells <= DPM_NOALLOC_MAX_CELLS and total vertices <=
+ *     DPM_NOALLOC_MAX_VERTICES, 3..256 vertices per cell; larger inputs are
+ *     rejected with DPM_ECAPACITY;
+ *   - every call shares that array: calls that overlap on the GPU (from two
+ *     threads, or on unordered streams) race; calls on one stream are safe;
+ *   - the first call on a device looks up the array's device address once.
+ * Work is enqueued on `stream` (a cudaStream_t; NULL for the default stream)
+ * and the call returns after it completes. */
+#define DPM_NOALLOC_MAX_CELLS 2048
+#define DPM_NOALLOC_MAX_VERTICES 65536
+int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *Ka,
+                       const float *Kl, const float *Kb, const float *a0,
+                       const float *l0, const float *r0, float L, float Kre,
+                       float Kat, int pbc, float *xy_dev, float *F_dev,
+                       int nsteps, float dt, void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* 3D batches                                                              */
 /* ---------------------------------------------------------------------- */
 
