@@ -20,10 +20,13 @@ outside the timed events.  value = vertices * simulation steps / time.
 
 Also reported: the plain single-tissue path on 1,024 bidisperse cells
 ("plain"), the dominant kernel's roofline, the end-to-end rate through the C
-ABI with pinned host buffers ("e2e"), SM clocks during the timed region and
-the CPU baseline (the oracle restatement of the reference on the host cores).
+ABI with pinned host buffers ("e2e"), the served mixed stream of 2D and 3D
+requests through dpm_serve_* with p50/p99 latency ("served"), SM clocks
+during the timed region and the CPU baseline (the oracle restatement of the
+reference on the host cores).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--serve-requests R]
 """
 from __future__ import annotations
 
@@ -100,6 +103,34 @@ def workload_plain(seed=1, n=1024):
     r0 = rng.permutation(np.r_[np.full(n // 2, 1.0), np.full(n - n // 2, 1.4)])
     calA = rng.uniform(1.0, 1.2, n)
     return [build_tissue(clDPM, rng, n, np.full(n, 32), calA, r0, 0.01, 0.6)]
+
+
+DT3 = 0.002  # 3D monolayer time step
+
+
+def build_monolayer(clDPM, rng, n, level, r0=1.0, calA=1.05):
+    """n icospheres (Cell3D ctor geometry) resting on z = 0, centres on a
+    jittered hexagonal lattice (spacing 2 r0, jitter U[-0.1, 0.1]) in a
+    periodic box; kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion range 0.1."""
+    proto = clDPM.Cell3D([0.0, 0.0, 0.0], calA, r0, level)
+    ring = np.asarray(proto.Verts, np.float32)
+    faces = np.asarray(proto.GetFaces(), np.uint32)
+    m = int(math.ceil(math.sqrt(n)))
+    sp = 2.0 * r0
+    L = np.float32(m * sp)
+    sites = rng.permutation(m * m)[:n]
+    ix, iy = sites % m, sites // m
+    cx = ((ix + 0.5 + 0.5 * (iy % 2)) * sp) % L + rng.uniform(-0.1, 0.1, n)
+    cy = (iy + 0.5) * sp + rng.uniform(-0.1, 0.1, n)
+    cen = np.stack([cx, cy, np.full(n, r0)], axis=1).astype(np.float32)
+    xyz = np.concatenate([ring + cen[i] for i in range(n)])
+    a0 = np.full(n, proto.a0, np.float32)
+    # the host model's rest edge: sqrt(double(4 a0)) / sqrt(3), 4 a0 in float
+    l0 = (np.sqrt((np.float32(4.0) * a0).astype(np.float64)) / np.sqrt(3.0)).astype(np.float32)
+    f = lambda v: np.full(n, v, np.float32)
+    return dict(dim=3, nv=int(proto.NV), faces=faces, xyz=xyz, Kv=f(1.0), Ka=f(0.5), Ks=f(0.1),
+                v0=f(proto.v0), a0=a0, l0=l0, Kb=f(0.05), adh=f(0.1), L=L, Kre=1.0,
+                level=level)
 
 
 def make_batch(ctx, tissues):
@@ -315,6 +346,10 @@ def run_ours(args, rank, world, local_rank):
                          "calA0 ~ U[1.0,1.2], kb=0.01, packing fraction 0.6 (static box)",
              "tuning": ptuned}
 
+    served = None
+    if args.serve_requests > 0:
+        served = run_served(ctx, value / world, args.serve_requests)
+
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
@@ -331,10 +366,149 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches_per_call(b, SIM_STEPS, tuned["rebuild_period"]) * args.steps,
         "roofline": roofline, "e2e": e2e, "plain": plain,
         "batched_over_plain": round(value / world / plain["value"], 2),
+        "served": served,
         "clocks": clock_info,
     }
     line["cpu_baseline"] = cpu_baseline(tissues, budget_s=args.cpu_budget)
     return line
+
+
+# ---------------------------------------------------------------------------
+# served mixed stream (continuous batching through dpm_serve_*)
+# ---------------------------------------------------------------------------
+
+SERVE_CHUNK = 256
+# (slots, cells per slot) of the 2D pools (NV <= 32) and of the 3D pools per
+# subdivision level; slot memory is small next to HBM, so the pools are sized
+# for concurrency
+POOLS_2D = [(48, 128), (32, 512), (24, 2048)]
+POOLS_3D = [(16, 128)]
+
+
+def served_requests(seed, nreq):
+    """70% 2D tissues drawn like the batched sweep with N ~ U{16..2048} and
+    NV in {16, 32}; 30% 3D monolayers with N ~ U{8..128} at subdivision 2 or
+    3; each runs U{1000..50000} steps."""
+    from opencl_dpm_gb300 import clDPM
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(nreq):
+        if rng.random() < 0.7:
+            n = int(rng.integers(16, 2049))
+            nv = int(rng.choice([16, 32]))
+            kb = float(10 ** rng.uniform(-3, -1))
+            calA = rng.uniform(1.0, 1.3, n)
+            phi = float(rng.uniform(0.6, 0.9))
+            t = build_tissue(clDPM, rng, n, np.full(n, nv), calA, np.ones(n), kb, phi)
+            t["dim"] = 2
+            t["verts"] = int(t["nv"].sum())
+        else:
+            n = int(rng.integers(8, 129))
+            t = build_monolayer(clDPM, rng, n, int(rng.choice([2, 3])))
+            t["verts"] = n * t["nv"]
+        t["steps"] = int(rng.integers(1000, 50001))
+        reqs.append(t)
+    return reqs
+
+
+def rate3d(ctx, level, steps=16):
+    """Vertex-steps/s of a 3D batch of 4 monolayers of 96 cells."""
+    import torch
+    from opencl_dpm_gb300 import clDPM
+    from opencl_dpm_gb300.abi import Batch3D
+    rng = np.random.default_rng(5)
+    ts = [build_monolayer(clDPM, rng, 96, level) for _ in range(4)]
+    cat = lambda k: np.concatenate([t[k] for t in ts])
+    b = Batch3D(ctx, [96] * 4, ts[0]["faces"], ts[0]["nv"])
+    b.set_cells(cat("Kv"), cat("Ka"), cat("Ks"), cat("v0"), cat("a0"), cat("l0"), cat("Kb"),
+                cat("adh"))
+    b.set_tissues([t["L"] for t in ts], 1.0, 1)
+    b.upload(cat("xyz"))
+    b.step(steps, DT3)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    b.step(steps, DT3)
+    ctx.synchronize()
+    secs = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    return b.nverts * steps / secs
+
+
+def run_served(ctx, rate2d, nreq, seed=77):
+    """Seeded Poisson arrivals at 80% of the device's measured capacity for
+    this request mix; latency = completion - arrival (host clock)."""
+    from opencl_dpm_gb300.abi import Server
+    reqs = served_requests(seed, nreq)
+    r3 = {lv: rate3d(ctx, lv) for lv in (2, 3)}
+    cost = [t["verts"] * t["steps"] / (rate2d if t["dim"] == 2 else r3[t["level"]]) for t in reqs]
+    lam = 0.8 / float(np.mean(cost))
+    rng = np.random.default_rng(seed + 1)
+    arrival = np.cumsum(rng.exponential(1.0 / lam, size=nreq))
+    arrival -= arrival[0]
+
+    srv = Server(ctx, hbm_budget_bytes=32 << 30, chunk_steps=SERVE_CHUNK)
+    for slots, cells in POOLS_2D:
+        srv.add_pool2d(slots, cells, 32, DT)
+    faces = {t["level"]: (t["faces"], t["nv"]) for t in reqs if t["dim"] == 3}
+    for lv, (f, nv) in sorted(faces.items()):
+        for slots, cells in POOLS_3D:
+            srv.add_pool3d(slots, cells, f, nv, DT3)
+    pool_bytes = srv.pool_bytes()
+
+    ids = [None] * nreq
+    done_at = np.zeros(nreq)
+    running = set()
+    nxt = 0
+    rounds = 0
+    t0 = time.perf_counter()
+    while nxt < nreq or running:
+        now = time.perf_counter() - t0
+        while nxt < nreq and arrival[nxt] <= now:
+            t = reqs[nxt]
+            if t["dim"] == 2:
+                ids[nxt] = srv.submit2d(t["nv"], t["Ka"], t["Kl"], t["Kb"], t["a0"], t["l0"],
+                                        t["r0"], t["xy"], float(t["L"]), t["Kre"], t["Kat"], 1,
+                                        t["steps"], DT)
+            else:
+                ids[nxt] = srv.submit3d(t["nv"], t["Kv"], t["Ka"], t["Ks"], t["v0"], t["a0"],
+                                        t["l0"], t["xyz"], float(t["L"]), t["Kre"], 1,
+                                        t["steps"], DT3, Kb=t["Kb"], adh=t["adh"])
+            running.add(nxt)
+            nxt += 1
+        if not running:
+            time.sleep(max(0.0, arrival[nxt] - (time.perf_counter() - t0)))
+            continue
+        srv.step()
+        rounds += 1
+        tnow = time.perf_counter() - t0
+        for i in list(running):
+            if srv.status(ids[i]) == 2:
+                done_at[i] = tnow
+                running.discard(i)
+                srv.forget(ids[i])
+    makespan = float(done_at.max())
+    lat = done_at - arrival
+    vs, _ = srv.stats()
+    srv.close()
+    n2 = sum(1 for t in reqs if t["dim"] == 2)
+    return {
+        "value": round(vs / makespan, 1), "unit": UNIT,
+        "latency_s": {"p50": round(float(np.percentile(lat, 50)), 4),
+                      "p99": round(float(np.percentile(lat, 99)), 4),
+                      "max": round(float(lat.max()), 4)},
+        "requests": nreq, "requests_2d": n2, "requests_3d": nreq - n2,
+        "vertex_steps": vs, "makespan_s": round(makespan, 3), "rounds": rounds,
+        "arrival_rate_per_s": round(lam, 3),
+        "load": "80% of capacity estimated from the measured batched 2D rate and 3D batch "
+                f"rates (level 2: {r3[2]:.3g}, level 3: {r3[3]:.3g} vertex-steps/s)",
+        "pools": {"2d": [{"slots": s, "cells": c, "nv_max": 32} for s, c in POOLS_2D],
+                  "3d": [{"slots": s, "cells": c} for s, c in POOLS_3D],
+                  "bytes": pool_bytes, "chunk_steps": SERVE_CHUNK},
+        "workload": "seeded Poisson arrivals; 70% 2D (N~U{16..2048}, NV in {16,32}, params as "
+                    "the batched sweep, dt=0.005), 30% 3D monolayers (N~U{8..128}, subdivision "
+                    "2 or 3, kv=1 ka=0.5 ks=0.1 kb=0.05 adhesion 0.1, dt=0.002); "
+                    "steps~U{1000..50000}",
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -409,6 +583,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--serve-requests", type=int, default=64,
+                    help="requests in the served mixed stream (0 skips it)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))

@@ -214,6 +214,53 @@ int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel);
  * reference's threshold in the last step (uint8 per vertex). */
 int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts);
 
+/* ---------------------------------------------------------------------- */
+/* Serving: continuous batching of independent simulation requests.       */
+/* The reference runs one Tissue per process, looping CLEulerUpdate        */
+/* (src/Tissue2D.cpp:116-241, src/Tissue3D.cpp:118-522); a server keeps     */
+/* many requests resident in slot pools and steps them together.           */
+/* ---------------------------------------------------------------------- */
+
+typedef struct dpm_server dpm_server;
+
+/* hbm_budget_bytes bounds the resident footprint of admitted requests;
+ * chunk_steps is the number of steps each round runs (a multiple of 16). */
+int dpm_serve_create(dpm_ctx *ctx, size_t hbm_budget_bytes, int chunk_steps,
+                     dpm_server **out);
+int dpm_serve_destroy(dpm_server *s);
+/* A pool of `slots` 2D tissues of up to cells_per_slot cells with up to
+ * nv_max vertices each, stepped with time step dt. */
+int dpm_serve_add_pool2d(dpm_server *s, int slots, int cells_per_slot,
+                         int nv_max, float dt);
+/* A pool of 3D tissues sharing one mesh (nv vertices, faces[nf*3]). */
+int dpm_serve_add_pool3d(dpm_server *s, int slots, int cells_per_slot, int nv,
+                         int nf, const unsigned *faces, float dt);
+int dpm_serve_pool_bytes(dpm_server *s, size_t *bytes);
+/* Queues one tissue for nsteps steps; the arguments mean what they mean in
+ * dpm2d_set_cells / dpm2d_set_tissues / dpm2d_upload for a batch of one
+ * tissue.  Fails with DPM_ECAPACITY when no pool can ever hold it. */
+int dpm_serve_submit2d(dpm_server *s, int ncells, const unsigned *nv,
+                       const float *Ka, const float *Kl, const float *Kb,
+                       const float *a0, const float *l0, const float *r0,
+                       const float *xy, float L, float Kre, float Kat, int pbc,
+                       int nsteps, float dt, uint64_t *id);
+int dpm_serve_submit3d(dpm_server *s, int ncells, int nv, const float *Kv,
+                       const float *Ka, const float *Ks, const float *v0,
+                       const float *a0, const float *l0, const float *Kb,
+                       const float *adh, const float *xyz, float L, float Kre,
+                       int pbc, int nsteps, float dt, uint64_t *id);
+/* One round: admit, step every pool by chunk_steps, retire finished
+ * requests.  Counts after the round are returned (any pointer may be NULL). */
+int dpm_serve_step(dpm_server *s, int *active, int *waiting, int *finished);
+/* status: 0 waiting, 1 running, 2 done.  When done, copies the final
+ * positions and the forces of the request's last step, and the time from
+ * submit to completion. */
+int dpm_serve_result(dpm_server *s, uint64_t id, float *x, float *F,
+                     double *latency_s, int *status);
+/* Drops a finished request's host copy. */
+int dpm_serve_forget(dpm_server *s, uint64_t id);
+int dpm_serve_stats(dpm_server *s, double *vertex_steps, size_t *resident_bytes);
+
 #ifdef __cplusplus
 }
 #endif

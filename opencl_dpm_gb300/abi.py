@@ -61,6 +61,28 @@ SIGNATURES = {
     "dpm3d_sizes": (ctypes.c_int, [_vp, _c_int_p, _c_long_p]),
     "dpm3d_last_winding": (ctypes.c_int, [_vp, _c_ubyte_p]),
     "dpm3d_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+    "dpm2d_step_noalloc": (ctypes.c_int, [ctypes.c_int, _c_uint_p] + [_c_float_p] * 6 +
+                           [ctypes.c_float] * 3 + [ctypes.c_int, _vp, _vp, ctypes.c_int,
+                                                   ctypes.c_float, _vp]),
+    "dpm_serve_create": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "dpm_serve_destroy": (ctypes.c_int, [_vp]),
+    "dpm_serve_add_pool2d": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_float]),
+    "dpm_serve_add_pool3d": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, _c_uint_p, ctypes.c_float]),
+    "dpm_serve_pool_bytes": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "dpm_serve_submit2d": (ctypes.c_int, [_vp, ctypes.c_int, _c_uint_p] + [_c_float_p] * 7 +
+                           [ctypes.c_float] * 3 + [ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                   ctypes.POINTER(ctypes.c_uint64)]),
+    "dpm_serve_submit3d": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int] + [_c_float_p] * 9 +
+                           [ctypes.c_float] * 2 + [ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                   ctypes.POINTER(ctypes.c_uint64)]),
+    "dpm_serve_step": (ctypes.c_int, [_vp, _c_int_p, _c_int_p, _c_int_p]),
+    "dpm_serve_result": (ctypes.c_int, [_vp, ctypes.c_uint64, _c_float_p, _c_float_p,
+                                        ctypes.POINTER(ctypes.c_double), _c_int_p]),
+    "dpm_serve_forget": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "dpm_serve_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_size_t)]),
 }
 
 _lib = None
@@ -320,6 +342,102 @@ class Batch3D:
     def close(self):
         if self.h:
             self.lib.dpm3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """dpm_server: continuous batching of independent tissue simulations on
+    resident slot pools (see dpm_serve_* in dpm_gb300.h)."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int, chunk_steps: int = 256):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = _vp()
+        check(self.lib.dpm_serve_create(ctx.h, int(hbm_budget_bytes), chunk_steps,
+                                        ctypes.byref(h)))
+        self.h = h
+        self._shape = {}
+
+    def add_pool2d(self, slots: int, cells_per_slot: int, nv_max: int, dt: float):
+        check(self.lib.dpm_serve_add_pool2d(self.h, slots, cells_per_slot, nv_max, dt))
+
+    def add_pool3d(self, slots: int, cells_per_slot: int, faces, nv: int, dt: float):
+        f = np.ascontiguousarray(faces, dtype=np.uint32)
+        check(self.lib.dpm_serve_add_pool3d(self.h, slots, cells_per_slot, nv, len(f),
+                                            f.ctypes.data_as(_c_uint_p), dt))
+
+    def pool_bytes(self) -> int:
+        v = ctypes.c_size_t()
+        check(self.lib.dpm_serve_pool_bytes(self.h, ctypes.byref(v)))
+        return v.value
+
+    def submit2d(self, nv, Ka, Kl, Kb, a0, l0, r0, xy, L, Kre, Kat, pbc, nsteps, dt) -> int:
+        nvu = np.ascontiguousarray(nv, dtype=np.uint32)
+        arrs = [_f32(x) for x in (Ka, Kl, Kb, a0, l0, r0, xy)]
+        rid = ctypes.c_uint64()
+        check(self.lib.dpm_serve_submit2d(self.h, len(nvu), nvu.ctypes.data_as(_c_uint_p),
+                                          *[fptr(a) for a in arrs], L, Kre, Kat, int(pbc),
+                                          nsteps, dt, ctypes.byref(rid)))
+        self._shape[rid.value] = (int(nvu.sum()), 2)
+        return rid.value
+
+    def submit3d(self, nv, Kv, Ka, Ks, v0, a0, l0, xyz, L, Kre, pbc, nsteps, dt, Kb=None,
+                 adh=None) -> int:
+        arrs = [_f32(x) for x in (Kv, Ka, Ks, v0, a0, l0)]
+        kb = None if Kb is None else _f32(Kb)
+        ad = None if adh is None else _f32(adh)
+        x = _f32(xyz)
+        rid = ctypes.c_uint64()
+        check(self.lib.dpm_serve_submit3d(self.h, len(arrs[0]), nv, *[fptr(a) for a in arrs],
+                                          None if kb is None else fptr(kb),
+                                          None if ad is None else fptr(ad), fptr(x), L, Kre,
+                                          int(pbc), nsteps, dt, ctypes.byref(rid)))
+        self._shape[rid.value] = (x.size // 3, 3)
+        return rid.value
+
+    def step(self):
+        """One round; returns (active, waiting, finished)."""
+        a, w, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self.lib.dpm_serve_step(self.h, ctypes.byref(a), ctypes.byref(w), ctypes.byref(f)))
+        return a.value, w.value, f.value
+
+    def status(self, rid: int) -> int:
+        st = ctypes.c_int()
+        check(self.lib.dpm_serve_result(self.h, rid, None, None, None, ctypes.byref(st)))
+        return st.value
+
+    def result(self, rid: int):
+        """(positions, forces, latency_s) of a finished request, else None."""
+        n, d = self._shape[rid]
+        x = np.empty((n, d), np.float32)
+        F = np.empty((n, d), np.float32)
+        lat = ctypes.c_double()
+        st = ctypes.c_int()
+        check(self.lib.dpm_serve_result(self.h, rid, fptr(x), fptr(F), ctypes.byref(lat),
+                                        ctypes.byref(st)))
+        if st.value != 2:
+            return None
+        return x, F, lat.value
+
+    def forget(self, rid: int):
+        check(self.lib.dpm_serve_forget(self.h, rid))
+        self._shape.pop(rid, None)
+
+    def stats(self):
+        vs = ctypes.c_double()
+        rb = ctypes.c_size_t()
+        check(self.lib.dpm_serve_stats(self.h, ctypes.byref(vs), ctypes.byref(rb)))
+        return vs.value, rb.value
+
+    def close(self):
+        if self.h:
+            self.lib.dpm_serve_destroy(self.h)
             self.h = None
 
     def __del__(self):

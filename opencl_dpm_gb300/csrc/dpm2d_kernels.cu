@@ -143,6 +143,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32)
   if (c >= ncells) return;
   const Cell2D cp = cells[c];
   const int n = (int)cp.nv;
+  if (n == 0) return;  // an empty slot
   for (int k = lane; k < n; k += 32) {
     const float2 v = pos[cp.voff + k];
     shx[w][k] = v.x;
@@ -213,12 +214,23 @@ __global__ void __launch_bounds__(256) k2d_binprep(Rebuild2DArgs a, int local_bi
     o->gminy = mny;
     o->gmaxy = mxy;
     a.stale[t] = 0;
+    // the tissue's share of the rebuild period that follows
+    if (a.block_len > 0) {
+      const int run = min(T.steps_left, a.block_len);
+      o->run_now = run;
+      if (T.steps_left < kStepsUnlimited) o->steps_left = T.steps_left - run;
+    }
   }
   const float inv = __fdiv_rn((float)nb, T.L);
   for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x) {
     const Geom2D g = a.geom[c];
     const int bx = bin_of(g.cx, T.L, inv, nb), by = bin_of(g.cy, T.L, inv, nb);
     a.keys[c] = ((uint32_t)t << local_bits) | (uint32_t)(by * nb + bx);
+    a.vals[c] = (uint32_t)c;
+  }
+  // empty slots sort after the tissue's cells
+  for (int c = T.cell_end + threadIdx.x; c < T.cell_cap; c += blockDim.x) {
+    a.keys[c] = ((uint32_t)t << local_bits) | ((1u << local_bits) - 1u);
     a.vals[c] = (uint32_t)c;
   }
 }
@@ -304,6 +316,10 @@ __global__ void __launch_bounds__(kNbWarps * 32) k2d_neighbors(Rebuild2DArgs a, 
   const int c = blockIdx.x * kNbWarps + w;
   if (c >= a.ncells) return;
   const Cell2D cp = a.cells[c];
+  if (cp.nv == 0) {  // an empty slot
+    if (lane == 0) a.nn[c] = 0;
+    return;
+  }
   const int t = (int)cp.tissue;
   const Tissue2D T = a.tissues[t];
   const Geom2D gi = a.geom[c];
@@ -405,9 +421,19 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
   unsigned char *sf = sh_f[w];
 
   const Cell2D cp = a.cells[c];
+  const int n = (int)cp.nv;
+  if (n == 0) return;  // an empty slot
   const int tid = (int)cp.tissue;
   const Tissue2D T = a.tissues[tid];
-  const int n = (int)cp.nv;
+  if (a.step_index >= T.run_now) {
+    // the tissue's step budget is spent: carry its state over unchanged
+    for (int k = lane; k < n; k += 32) a.pos_out[cp.voff + k] = a.pos_in[cp.voff + k];
+    if (lane == 0) a.geom_out[c] = a.geom_in[c];
+    return;
+  }
+  // outputs of this step: for every cell when asked, else at the tissue's last step
+  const bool write_out =
+      a.all_forces != 0 || (a.step_index == T.run_now - 1 && T.steps_left == 0);
   const float L = T.L;
   const bool pbc = T.pbc != 0;
 
@@ -447,9 +473,12 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
       const float ax = ka * (ym - yp), ay = ka * (xm - xp);
       const float lvx = xp - x, lvy = yp - y, lmx = x - xm, lmy = y - ym;
       const float len = sqrtf(lvx * lvx + lvy * lvy), lenm = sqrtf(lmx * lmx + lmy * lmy);
-      const float dl = len / cp.l0 - 1.0f, dlm = lenm / cp.l0 - 1.0f;
-      const float px = cp.kL * (dl * (lvx / len) - dlm * (lmx / lenm));
-      const float py = cp.kL * (dl * (lvy / len) - dlm * (lmy / lenm));
+      // unit vectors and strains with reciprocals (within 1 ulp of the
+      // reference's divisions)
+      const float il = 1.0f / len, ilm = 1.0f / lenm;
+      const float dl = len * cp.inv_l0 - 1.0f, dlm = lenm * cp.inv_l0 - 1.0f;
+      const float px = cp.kL * (dl * (lvx * il) - dlm * (lmx * ilm));
+      const float py = cp.kL * (dl * (lvy * il) - dlm * (lmy * ilm));
       const float six = lvx - lmx, siy = lvy - lmy;
       const float sixp = (xpp - xp) - lvx, siyp = (ypp - yp) - lvy;
       const float sixm = lmx - (xm - xmm), siym = lmy - (ym - ymm);
@@ -552,18 +581,18 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
     }
     if (!anyc && !anya) continue;
 
-    // stage the neighbour's ring
     const uint4 jr = *reinterpret_cast<const uint4 *>(a.cells + j);
     const int nj = (int)jr.y;
     const float2 *pj = a.pos_in + jr.x;
-    for (int k = lane; k < nj; k += 32) {
-      const float2 v = pj[k];
-      nxs[k] = v.x;
-      nys[k] = v.y;
-    }
-    __syncwarp();
 
     if (anya) {
+      // stage the neighbour's ring for the per-vertex attraction loops
+      for (int k = lane; k < nj; k += 32) {
+        const float2 v = pj[k];
+        nxs[k] = v.x;
+        nys[k] = v.y;
+      }
+      __syncwarp();
       // AttractionForceUpdate (Cell2D_kernel.cl:251-267)
       const float kat = T.Kat / (float)n;
 #pragma unroll
@@ -588,22 +617,44 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
     }
     if (anyc) {
       // RepulsionForceUpdate containment (Cell2D_kernel.cl:166-202):
-      // lanes take the edges, a ballot gives the crossing parity.
+      // lanes take the edges (P_e, P_{e-1}) of the neighbour, held in
+      // registers for all candidates; a ballot gives the crossing parity.
+      // Edges can be shifted only for "far" pairs, so the plain test is
+      // used otherwise.
+      float ex[S], ey[S], qx[S], qy[S];
+#pragma unroll
+      for (int s2 = 0; s2 < S; ++s2) {
+        const int e = lane + 32 * s2;
+        ex[s2] = ey[s2] = qx[s2] = qy[s2] = 0.0f;
+        if (e < nj) {
+          const float2 p = pj[e], pp = pj[e == 0 ? nj - 1 : e - 1];
+          ex[s2] = p.x;
+          ey[s2] = p.y;
+          qx[s2] = pp.x;
+          qy[s2] = pp.y;
+        }
+      }
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         unsigned msk = cm[s];
         while (msk) {
           const int l = __ffs(msk) - 1;
           msk &= msk - 1u;
-          const int v = l + 32 * s;
-          const float X = sx[v], Y = sy[v];
+          const float X = __shfl_sync(kFull, vx[s], l), Y = __shfl_sync(kFull, vy[s], l);
           unsigned par = 0u;
-          for (int e = lane; e < nj; e += 32) {
-            const int ep = e == 0 ? nj - 1 : e - 1;
-            par ^= edge_crosses(X, Y, nxs[e], nys[e], nxs[ep], nys[ep], pbc, L);
+          if (far) {
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2)
+              if (lane + 32 * s2 < nj)
+                par ^= edge_crosses(X, Y, ex[s2], ey[s2], qx[s2], qy[s2], true, L);
+          } else {
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2)
+              if (lane + 32 * s2 < nj)
+                par ^= edge_crosses(X, Y, ex[s2], ey[s2], qx[s2], qy[s2], false, L);
           }
           const unsigned bal = __ballot_sync(kFull, par != 0u);
-          if ((__popc(bal) & 1) && lane == 0) sf[v] = 1;
+          if ((__popc(bal) & 1) && lane == 0) sf[l + 32 * s] = 1;
         }
       }
     }
@@ -617,17 +668,17 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
     const int k = lane + 32 * s;
     if (k < n && sf[k]) {
       float dx = gi.cx - vx[s], dy = gi.cy - vy[s];
-      if (pbc) {
-        dx -= L * roundf(dx / L);
-        dy -= L * roundf(dy / L);
-      }
-      const float dist = sqrtf(dx * dx + dy * dy);
-      const float xij = dist / (2.0f * cp.r0);
+      // d -= L*round(d/L); for |d| <= 0.49 L the rounded quotient is 0
+      if (pbc && fabsf(dx) > 0.49f * L) dx -= L * roundf(dx / L);
+      if (pbc && fabsf(dy) > 0.49f * L) dy -= L * roundf(dy / L);
+      const float d2 = dx * dx + dy * dy;
+      const float dist = sqrtf(d2);
+      const float xij = dist * cp.inv_2r0;
       const float ftmp = T.Kre * (1.0f - xij);
-      float ux, uy;
-      normalize2(dx, dy, ux, uy);
-      fx[s] += 0.5f * ftmp * ux;
-      fy[s] += 0.5f * ftmp * uy;
+      // normalize(d), with the zero vector mapped to itself
+      const float inv = d2 == 0.0f ? 1.0f : 1.0f / dist;
+      fx[s] += 0.5f * ftmp * (dx * inv);
+      fy[s] += 0.5f * ftmp * (dy * inv);
     }
   }
 
@@ -639,8 +690,8 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
       const float nxv = __fadd_rn(vx[s], __fmul_rn(fx[s], a.dt));
       const float nyv = __fadd_rn(vy[s], __fmul_rn(fy[s], a.dt));
       a.pos_out[cp.voff + k] = make_float2(nxv, nyv);
-      if (a.force_out) a.force_out[cp.voff + k] = make_float2(fx[s], fy[s]);
-      if (a.flags_out) a.flags_out[cp.voff + k] = sf[k];
+      if (a.force_out && write_out) a.force_out[cp.voff + k] = make_float2(fx[s], fy[s]);
+      if (a.flags_out && write_out) a.flags_out[cp.voff + k] = sf[k];
       sx[k] = nxv;
       sy[k] = nyv;
     }

@@ -21,6 +21,9 @@ struct Step2DArgs {
   int *err;                 // bit 0: non-finite positions
   int ncells;
   float dt;
+  int step_index;  // index of this step within its rebuild period
+  int all_forces;  // 1: force_out/flags_out take every cell's values; 0: only
+                   // those of tissues whose step budget ends at this step
 };
 
 struct Rebuild2DArgs {
@@ -37,6 +40,7 @@ struct Rebuild2DArgs {
   int *stale;
   int ncells;
   int ntissues;
+  int block_len;  // steps in the rebuild period that follows (0: leave budgets)
 };
 
 // Geometry of every cell (circle, area, box) from positions.

@@ -174,9 +174,22 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
   const bool bend_any = a.bend != 0;
   Smem3D s = carve(smem3d, NV, NF, bend_any);
   const Cell3D P = a.cells[c];
+  if (!P.active) return;  // an empty slot (uniform over the block)
   const Tissue3D T = a.tissues[P.tissue];
   const size_t base = (size_t)c * NV;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (a.step_index >= T.run_now) {
+    // the tissue's step budget is spent: carry its state over unchanged
+    for (int v = tid; v < NV; v += kThreads) {
+      a.xout[base + v] = a.xin[base + v];
+      a.yout[base + v] = a.yin[base + v];
+      a.zout[base + v] = a.zin[base + v];
+    }
+    if (tid == 0) a.geom_out[c] = a.geom_in[c];
+    return;
+  }
+  const bool write_out =
+      a.all_forces != 0 || (a.step_index == T.run_now - 1 && T.steps_left == 0);
 
   for (int v = tid; v < NV; v += kThreads) {
     s.px[v] = a.xin[base + v];
@@ -393,12 +406,12 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
     a.xout[base + v] = nx;
     a.yout[base + v] = ny;
     a.zout[base + v] = nz;
-    if (a.fx) {
+    if (a.fx && write_out) {
       a.fx[base + v] = s.fx[v];
       a.fy[base + v] = s.fy[v];
       a.fz[base + v] = s.fz[v];
     }
-    if (a.wn_out) a.wn_out[base + v] = s.wnc[v];
+    if (a.wn_out && write_out) a.wn_out[base + v] = s.wnc[v];
     s.px[v] = nx;
     s.py[v] = ny;
     s.pz[v] = nz;
@@ -421,8 +434,9 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
 
 __global__ void __launch_bounds__(kThreads)
     k3d_geom(const float *x, const float *y, const float *z, const uint16_t *faces, int nf,
-             Geom3D *geom, int nv) {
+             const Cell3D *cells, Geom3D *geom, int nv) {
   __shared__ float px[kMaxNV3D], py[kMaxNV3D], pz[kMaxNV3D], red[64];
+  if (!cells[blockIdx.x].active) return;  // an empty slot
   const size_t base = (size_t)blockIdx.x * nv;
   for (int v = threadIdx.x; v < nv; v += kThreads) {
     px[v] = x[base + v];
@@ -464,6 +478,12 @@ __global__ void __launch_bounds__(256) k3d_binprep(Rebuild3DArgs a, int local_bi
     a.tissues[t].nb = nb;
     a.tissues[t].binw = wdt;
     a.stale[t] = 0;
+    // the tissue's share of the rebuild period that follows
+    if (a.block_len > 0) {
+      const int run = min(T.steps_left, a.block_len);
+      a.tissues[t].run_now = run;
+      if (T.steps_left < kStepsUnlimited) a.tissues[t].steps_left = T.steps_left - run;
+    }
   }
   const float inv = __fdiv_rn((float)nb, T.L);
   for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x) {
@@ -471,6 +491,11 @@ __global__ void __launch_bounds__(256) k3d_binprep(Rebuild3DArgs a, int local_bi
     const int bx = bin3(g.cx, T.L, inv, nb), by = bin3(g.cy, T.L, inv, nb),
               bz = bin3(g.cz, T.L, inv, nb);
     a.keys[c] = ((uint32_t)t << local_bits) | (uint32_t)((bz * nb + by) * nb + bx);
+    a.vals[c] = (uint32_t)c;
+  }
+  // empty slots sort after the tissue's cells
+  for (int c = T.cell_end + threadIdx.x; c < T.cell_cap; c += blockDim.x) {
+    a.keys[c] = ((uint32_t)t << local_bits) | ((1u << local_bits) - 1u);
     a.vals[c] = (uint32_t)c;
   }
 }
@@ -511,6 +536,10 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * kNb3Warps + w;
   if (c >= a.ncells) return;
+  if (!a.cells[c].active) {  // an empty slot
+    if (lane == 0) a.nn[c] = 0;
+    return;
+  }
   const int t = (int)a.cells[c].tissue;
   const Tissue3D T = a.tissues[t];
   const Geom3D gi = a.geom[c];
@@ -592,8 +621,8 @@ cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_geom3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
-                          Geom3D *geom, int ncells, cudaStream_t s) {
-  k3d_geom<<<ncells, kThreads, 0, s>>>(x, y, z, mesh.faces, mesh.nf, geom, mesh.nv);
+                          const Cell3D *cells, Geom3D *geom, int ncells, cudaStream_t s) {
+  k3d_geom<<<ncells, kThreads, 0, s>>>(x, y, z, mesh.faces, mesh.nf, cells, geom, mesh.nv);
   return cudaGetLastError();
 }
 

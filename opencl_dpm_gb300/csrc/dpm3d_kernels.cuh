@@ -31,6 +31,8 @@ struct Step3DArgs {
   int ncells;
   float dt;
   int bend; // any cell with Kb != 0
+  int step_index; // index of this step within its rebuild period
+  int all_forces; // 1: outputs for every cell; 0: only at each tissue's last step
 };
 
 struct Rebuild3DArgs {
@@ -42,10 +44,11 @@ struct Rebuild3DArgs {
   const uint32_t *sorted_keys, *sorted_vals;
   int *nn, *nbr, *stale;
   int ncells, ntissues;
+  int block_len; // steps in the rebuild period that follows (0: leave budgets)
 };
 
 cudaError_t launch_geom3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
-                          Geom3D *geom, int ncells, cudaStream_t s);
+                          const Cell3D *cells, Geom3D *geom, int ncells, cudaStream_t s);
 cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 size_t step3d_smem_bytes(int nv, int nf, bool bend);

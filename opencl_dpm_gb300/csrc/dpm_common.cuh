@@ -34,20 +34,29 @@ struct alignas(16) Cell2D {
   uint32_t tissue; // owning tissue
   uint32_t pad0;
   float a0, l0, kA, kL;
-  float Kb, r0, pad1, pad2;
+  float Kb, r0;
+  float inv_l0;  // 1 / l0
+  float inv_2r0; // 1 / (2 r0)
 };
 
 // Per-tissue constants and cell-list state of a 2D tissue (80 bytes).
 struct alignas(16) Tissue2D {
   float L, Kre, Kat, l0max;  // l0max: largest l0 (attraction range)
   int pbc;
-  int cell_begin, cell_end;  // [begin, end) in batch cell order
+  int cell_begin, cell_end;  // active cells [begin, end) in batch cell order
   int cap;                   // upper bound on bins per axis
   float skin;                // neighbour-list skin (absolute)
   float binw;                // bin width of the last rebuild
   int nbx, nby;              // bins per axis of the last rebuild
   float gminx, gmaxx, gminy, gmaxy; // raw extent at the last rebuild
+  int cell_cap;   // end of the tissue's cell slots (>= cell_end)
+  int steps_left; // step budget; each rebuild takes run_now steps from it
+  int run_now;    // steps of the current rebuild period this tissue runs
+  int pad;
 };
+
+// A step budget that never runs out (ordinary batches).
+constexpr int kStepsUnlimited = 0x3fffffff;
 
 // Per-cell geometry at the current positions: circle (centre, radius)
 // around the vertices, the cell area, and the axis-aligned box.
@@ -71,12 +80,14 @@ struct alignas(16) Cell3D {
   float Kv, Ka, Ks, v0;
   float a0, l0, Kb, adh;
   float sa_scale;
-  uint32_t tissue, pad0, pad1;
+  uint32_t tissue;
+  uint32_t active; // 0: an empty slot
+  uint32_t pad1;
 };
 struct alignas(16) Tissue3D {
   float L, Kre, skin, binw;
-  int pbc, cell_begin, cell_end, cap;
-  int nb, pad0, pad1, pad2;
+  int pbc, cell_begin, cell_end, cap; // active cells [begin, end)
+  int nb, cell_cap, steps_left, run_now;
 };
 // Centre of mass, largest vertex distance from it, and the longest mesh
 // edge (the reference's winding sum drops faces whose denominator is below

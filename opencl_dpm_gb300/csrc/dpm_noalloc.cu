@@ -151,6 +151,8 @@ extern "C" int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *K
     C.kL = Kl[c] * std::sqrt(a0[c] / l0[c]);
     C.Kb = Kb[c];
     C.r0 = r0[c];
+    C.inv_l0 = 1.0f / l0[c];
+    C.inv_2r0 = 1.0f / (2.0f * r0[c]);
     off += nv[c];
   }
   Tissue2D T;
@@ -168,6 +170,9 @@ extern "C" int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *K
   cap = std::max(1L, std::min(cap, (long)kMaxBinsAxis));
   T.cap = (int)cap;
   T.nbx = T.nby = 1;
+  T.cell_cap = ncells;
+  T.steps_left = kStepsUnlimited;
+  T.run_now = kStepsUnlimited;
   const int local_bits = std::max(1, ceil_log2i(cap * cap));
 
   // everything that must start at zero: neighbour counts, stale and error flags
@@ -197,6 +202,7 @@ extern "C" int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *K
   for (int done = 0; done < nsteps;) {
     const int len = std::min(kPeriod, nsteps - done);
     rb.geom = geom[cur];
+    rb.block_len = len;
     DPM_CUDA_TRY(launch_binprep2d(rb, local_bits, s));
     bool alt = false;
     DPM_CUDA_TRY(radix_sort_pairs(keys, vals, keys_alt, vals_alt, ncells, local_bits,
@@ -221,6 +227,8 @@ extern "C" int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *K
       a.err = err;
       a.ncells = ncells;
       a.dt = dt;
+      a.step_index = i;
+      a.all_forces = 1;
       DPM_CUDA_TRY(launch_step2d(a, maxnv, 8, 1, s));
       cur = 1 - cur;
     }

@@ -17,11 +17,44 @@ struct dpm_ctx {
   std::atomic<int> refs{1};
 };
 
+struct dpm2d_batch;
+struct dpm3d_batch;
+
 namespace dpm {
 
 const char *last_error();
 void ctx_retain(dpm_ctx *ctx);
 void ctx_release(dpm_ctx *ctx);
+
+// ---- slot pools (the server's resident state) ----
+// A pool is a batch whose tissues are fixed-capacity slots: a request is
+// written into a free slot, runs under a per-tissue step budget inside the
+// pool's shared graphs (finished slots freeze in place), and is read back
+// and released.  Each pool runs on its own stream.
+
+int pool2d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv_max, dpm2d_batch **out);
+int pool2d_assign(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, const float *Ka,
+                  const float *Kl, const float *Kb, const float *a0, const float *l0,
+                  const float *r0, const float *xy, float L, float Kre, float Kat, int pbc,
+                  int nsteps);
+int pool2d_run(dpm2d_batch *b, int nsteps, float dt);  // enqueue only
+int pool2d_fetch(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, float *xy,
+                 float *F);  // synchronizes the pool's stream
+int pool2d_release(dpm2d_batch *b, int slot);
+int pool2d_sync(dpm2d_batch *b);
+size_t pool2d_bytes(const dpm2d_batch *b);
+
+int pool3d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv, int nf,
+                  const unsigned *faces, dpm3d_batch **out);
+int pool3d_assign(dpm3d_batch *b, int slot, int ncells, const float *Kv, const float *Ka,
+                  const float *Ks, const float *v0, const float *a0, const float *l0,
+                  const float *Kb, const float *adh, const float *xyz, float L, float Kre,
+                  int pbc, int nsteps);
+int pool3d_run(dpm3d_batch *b, int nsteps, float dt);
+int pool3d_fetch(dpm3d_batch *b, int slot, int ncells, float *xyz, float *F);
+int pool3d_release(dpm3d_batch *b, int slot);
+int pool3d_sync(dpm3d_batch *b);
+size_t pool3d_bytes(const dpm3d_batch *b);
 
 // One device allocation carved into 256-byte aligned arrays.  A batch owns
 // its arena; nothing else allocates on the step path.

@@ -68,6 +68,8 @@ using namespace dpm;
 
 struct dpm2d_batch {
   dpm_ctx *ctx = nullptr;
+  cudaStream_t stream = nullptr; // the context's, or the pool's own
+  bool own_stream = false;
   int ntissues = 0, ncells = 0, maxnv = 0;
   long nverts = 0;
   std::vector<int> tissue_ncells;
@@ -96,11 +98,18 @@ struct dpm2d_batch {
   float skin_rel = 0.15f;
   int warps = 8;
   int occ = 1;
+  bool serving = false; // slot pool of a server: per-tissue step budgets
   long rebuilds = 0;
 
   std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
 
-  ~dpm2d_batch() { clear_graphs(); }
+  ~dpm2d_batch() {
+    clear_graphs();
+    if (own_stream && stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+  }
   void clear_graphs() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
@@ -124,10 +133,12 @@ struct dpm2d_batch {
     return a;
   }
 
-  // Enqueue one neighbour-list rebuild on geometry buffer `g`.
-  cudaError_t enqueue_rebuild(int g, cudaStream_t s) {
+  // Enqueue one neighbour-list rebuild on geometry buffer `g`, for a rebuild
+  // period of block_len steps (0: leave the step budgets untouched).
+  cudaError_t enqueue_rebuild(int g, int block_len, cudaStream_t s) {
     Rebuild2DArgs a = rebuild_args();
     a.geom = d_geom[g];
+    a.block_len = block_len;
     cudaError_t e = launch_binprep2d(a, local_bits, s);
     if (e != cudaSuccess) return e;
     bool alt = false;
@@ -140,14 +151,23 @@ struct dpm2d_batch {
     return launch_neighbors2d(a, local_bits, s);
   }
 
-  Step2DArgs step_args(int from, float dt, bool last) const {
+  Step2DArgs step_args(int from, float dt, bool last, int index) const {
     Step2DArgs a{};
     a.cells = d_cells;
     a.tissues = d_tissues;
     a.pos_in = d_pos[from];
     a.pos_out = d_pos[1 - from];
-    a.force_out = last ? d_force : nullptr;
-    a.flags_out = last ? d_flags : nullptr;
+    if (serving) {
+      // each tissue stores its outputs at the last step of its own budget
+      a.force_out = d_force;
+      a.flags_out = d_flags;
+      a.all_forces = 0;
+    } else {
+      a.force_out = last ? d_force : nullptr;
+      a.flags_out = last ? d_flags : nullptr;
+      a.all_forces = 1;
+    }
+    a.step_index = index;
     a.geom_in = d_geom[from];
     a.geom_out = d_geom[1 - from];
     a.geom0 = d_geom0;
@@ -162,11 +182,11 @@ struct dpm2d_batch {
 
   // Enqueue a block: rebuild, then `len` steps starting from buffer `from`.
   cudaError_t enqueue_block(int len, int from, float dt, bool last, cudaStream_t s) {
-    cudaError_t e = enqueue_rebuild(from, s);
+    cudaError_t e = enqueue_rebuild(from, len, s);
     if (e != cudaSuccess) return e;
     int f = from;
     for (int i = 0; i < len; ++i) {
-      e = launch_step2d(step_args(f, dt, last && i == len - 1), maxnv, warps, occ, s);
+      e = launch_step2d(step_args(f, dt, last && i == len - 1, i), maxnv, warps, occ, s);
       if (e != cudaSuccess) return e;
       f = 1 - f;
     }
@@ -174,7 +194,7 @@ struct dpm2d_batch {
   }
 
   int run_block(int len, float dt, bool last) {
-    cudaStream_t s = ctx->stream;
+    cudaStream_t s = stream;
     uint32_t dtbits;
     std::memcpy(&dtbits, &dt, 4);
     auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0);
@@ -269,6 +289,7 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
   try {
     auto b = std::make_unique<dpm2d_batch>();
     b->ctx = ctx;
+    b->stream = ctx->stream;
     b->ntissues = ntissues;
     long total_cells = 0;
     for (int t = 0; t < ntissues; ++t) {
@@ -300,6 +321,9 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
       T.cell_end = cb + ncells[t];
       T.cap = 1;
       T.nbx = T.nby = 1;
+      T.cell_cap = T.cell_end;
+      T.steps_left = kStepsUnlimited;
+      T.run_now = kStepsUnlimited;
       for (int c = cb; c < cb + ncells[t]; ++c) {
         Cell2D &C = b->h_cells[c];
         std::memset(&C, 0, sizeof(C));
@@ -350,7 +374,7 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
 int dpm2d_destroy(dpm2d_batch *b) {
   if (!b) return DPM_OK;
   cudaSetDevice(b->ctx->device);
-  cudaStreamSynchronize(b->ctx->stream);
+  cudaStreamSynchronize(b->stream);
   dpm_ctx *c = b->ctx;
   delete b;
   ctx_release(c);
@@ -379,6 +403,8 @@ int dpm2d_set_cells(dpm2d_batch *b, const float *Ka, const float *Kl, const floa
     C.kL = Kl[c] * std::sqrt(a0[c] / l0[c]);
     C.Kb = Kb[c];
     C.r0 = r0[c];
+    C.inv_l0 = 1.0f / l0[c];
+    C.inv_2r0 = 1.0f / (2.0f * r0[c]);
   }
   // attraction range, skin and bin cap depend on the cells of each tissue
   for (int t = 0; t < b->ntissues; ++t) {
@@ -395,14 +421,14 @@ int dpm2d_set_cells(dpm2d_batch *b, const float *Ka, const float *Kl, const floa
   }
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells, b->h_cells.data(), sizeof(Cell2D) * b->ncells,
-                               cudaMemcpyHostToDevice, b->ctx->stream));
+                               cudaMemcpyHostToDevice, b->stream));
   b->cells_set = true;
   if (b->tissues_set) {
     DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
                                  sizeof(Tissue2D) * b->ntissues, cudaMemcpyHostToDevice,
-                                 b->ctx->stream));
+                                 b->stream));
   }
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DPM_OK;
 }
 
@@ -432,8 +458,8 @@ int dpm2d_set_tissues(dpm2d_batch *b, const float *L, const float *Kre, const fl
   if (b->key_bits > 32) return fail(DPM_ECAPACITY, "cell-list keys exceed 32 bits");
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue2D) * b->ntissues,
-                               cudaMemcpyHostToDevice, b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                               cudaMemcpyHostToDevice, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->tissues_set = true;
   b->clear_graphs();
   return DPM_OK;
@@ -463,8 +489,8 @@ int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel, int war
       cudaSetDevice(b->ctx->device);
       DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
                                    sizeof(Tissue2D) * b->ntissues, cudaMemcpyHostToDevice,
-                                   b->ctx->stream));
-      DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                                   b->stream));
+      DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
     }
   }
   return DPM_OK;
@@ -475,7 +501,7 @@ int dpm2d_upload(dpm2d_batch *b, const float *xy) {
   if (!xy) return fail(DPM_EINVAL, "null positions");
   if (!b->cells_set) return fail(DPM_ESTATE, "set the cell constants before uploading");
   cudaSetDevice(b->ctx->device);
-  cudaStream_t s = b->ctx->stream;
+  cudaStream_t s = b->stream;
   b->cur = 0;
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_pos[0], xy, sizeof(float2) * b->nverts,
                                cudaMemcpyHostToDevice, s));
@@ -492,8 +518,8 @@ int dpm2d_step_kernel(dpm2d_batch *b, float dt) {
   if (int r = check_batch(b)) return r;
   if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before stepping");
   cudaSetDevice(b->ctx->device);
-  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true), b->maxnv, b->warps, b->occ,
-                             b->ctx->stream));
+  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true, 0), b->maxnv, b->warps, b->occ,
+                             b->stream));
   b->cur = 1 - b->cur;
   return DPM_OK;
 }
@@ -519,7 +545,7 @@ int dpm2d_download(dpm2d_batch *b, float *xy, float *F) {
   if (int r = check_batch(b)) return r;
   if (!b->uploaded) return fail(DPM_ESTATE, "nothing uploaded");
   cudaSetDevice(b->ctx->device);
-  cudaStream_t s = b->ctx->stream;
+  cudaStream_t s = b->stream;
   if (xy)
     DPM_CUDA_TRY(cudaMemcpyAsync(xy, b->d_pos[b->cur], sizeof(float2) * b->nverts,
                                  cudaMemcpyDeviceToHost, s));
@@ -538,8 +564,8 @@ int dpm2d_last_contained(dpm2d_batch *b, unsigned char *flags) {
   if (!flags) return fail(DPM_EINVAL, "null output");
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(flags, b->d_flags, b->nverts, cudaMemcpyDeviceToHost,
-                               b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                               b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DPM_OK;
 }
 
@@ -549,8 +575,8 @@ int dpm2d_cell_areas(dpm2d_batch *b, float *area) {
   std::vector<Geom2D> g(b->ncells);
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(g.data(), b->d_geom[b->cur], sizeof(Geom2D) * b->ncells,
-                               cudaMemcpyDeviceToHost, b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                               cudaMemcpyDeviceToHost, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   for (int c = 0; c < b->ncells; ++c) area[c] = g[c].area;
   return DPM_OK;
 }
@@ -562,8 +588,8 @@ int dpm2d_stats(dpm2d_batch *b, long *rebuilds, long *fallback_steps) {
     std::vector<int> st(b->ntissues);
     cudaSetDevice(b->ctx->device);
     DPM_CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_stale, sizeof(int) * b->ntissues,
-                                 cudaMemcpyDeviceToHost, b->ctx->stream));
-    DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                                 cudaMemcpyDeviceToHost, b->stream));
+    DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
     long n = 0;
     for (int v : st) n += v ? 1 : 0;
     *fallback_steps = n;
@@ -575,8 +601,8 @@ int dpm2d_rebuild_now(dpm2d_batch *b) {
   if (int r = check_batch(b)) return r;
   if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before rebuilding");
   cudaSetDevice(b->ctx->device);
-  DPM_CUDA_TRY(b->enqueue_rebuild(b->cur, b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  DPM_CUDA_TRY(b->enqueue_rebuild(b->cur, 0, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DPM_OK;
 }
 
@@ -584,7 +610,7 @@ int dpm2d_cell_list(dpm2d_batch *b, unsigned *keys, unsigned *ids, int *nn, int 
                     int *maxnb, float *geom) {
   if (int r = check_batch(b)) return r;
   cudaSetDevice(b->ctx->device);
-  cudaStream_t s = b->ctx->stream;
+  cudaStream_t s = b->stream;
   const size_t N = b->ncells;
   if (keys)
     DPM_CUDA_TRY(cudaMemcpyAsync(keys, b->sorted_in_alt ? b->d_keys_alt : b->d_keys,
@@ -678,7 +704,7 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache, in
     return fail(DPM_ESTATE, "set cells and tissues and upload before tuning");
   if (trial_blocks <= 0) trial_blocks = 2;
   cudaSetDevice(b->ctx->device);
-  cudaStream_t s = b->ctx->stream;
+  cudaStream_t s = b->stream;
   const std::string key = tune_key(b, b->ctx->sm_count);
   int w = 0, o = 0, p = 0;
   float sk = 0.0f, best_ms = -1.0f;
@@ -779,8 +805,8 @@ int dpm2d_bins(dpm2d_batch *b, int *local_bits, int *nbins, float *binw, float *
   std::vector<Tissue2D> T(b->ntissues);
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(T.data(), b->d_tissues, sizeof(Tissue2D) * b->ntissues,
-                               cudaMemcpyDeviceToHost, b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                               cudaMemcpyDeviceToHost, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (local_bits) *local_bits = b->local_bits;
   for (int t = 0; t < b->ntissues; ++t) {
     if (nbins) nbins[t] = T[t].nbx;
@@ -791,3 +817,187 @@ int dpm2d_bins(dpm2d_batch *b, int *local_bits, int *nbins, float *binw, float *
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Slot pools for the server
+// ---------------------------------------------------------------------------
+
+namespace dpm {
+
+int pool2d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv_max, dpm2d_batch **out) {
+  if (nslots <= 0 || cells_per_slot <= 0) return fail(DPM_EINVAL, "empty pool");
+  if (nv_max < 3 || nv_max > kMaxNV2D) return fail(DPM_EINVAL, "pool nv_max must be 3..256");
+  std::vector<int> nc(nslots, cells_per_slot);
+  std::vector<unsigned> nv((size_t)nslots * cells_per_slot, (unsigned)nv_max);
+  dpm2d_batch *b = nullptr;
+  if (int r = dpm2d_create(ctx, nslots, nc.data(), nv.data(), &b)) return r;
+  b->serving = true;
+  // every cell starts as an empty slot; vertex storage stays strided by nv_max
+  for (auto &C : b->h_cells) C.nv = 0;
+  for (auto &T : b->h_tissues) {
+    T.cell_cap = T.cell_end;
+    T.cell_end = T.cell_begin;
+    T.L = 1.0f;
+    T.cap = 1;
+    T.steps_left = 0;
+    T.run_now = 0;
+  }
+  // bins per axis are capped at 1024, so local bin indices fit 20 bits
+  b->local_bits = 20;
+  b->key_bits = 20 + ceil_log2(nslots);
+  if (b->key_bits > 32) {
+    dpm2d_destroy(b);
+    return fail(DPM_ECAPACITY, "too many slots for 32-bit cell-list keys");
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    b->stream = ctx->stream;
+    dpm2d_destroy(b);
+    return cuda_fail(e, "pool stream");
+  }
+  b->own_stream = true;
+  e = cudaMemcpyAsync(b->d_cells, b->h_cells.data(), sizeof(Cell2D) * b->ncells,
+                      cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue2D) * b->ntissues,
+                        cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) {
+    dpm2d_destroy(b);
+    return cuda_fail(e, "pool upload");
+  }
+  b->cells_set = b->tissues_set = b->uploaded = true;
+  *out = b;
+  return DPM_OK;
+}
+
+size_t pool2d_bytes(const dpm2d_batch *b) { return b->arena.capacity(); }
+
+int pool2d_assign(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, const float *Ka,
+                  const float *Kl, const float *Kb, const float *a0, const float *l0,
+                  const float *r0, const float *xy, float L, float Kre, float Kat, int pbc,
+                  int nsteps) {
+  if (slot < 0 || slot >= b->ntissues) return fail(DPM_EINVAL, "no such slot");
+  Tissue2D &T = b->h_tissues[slot];
+  const int cap_cells = T.cell_cap - T.cell_begin;
+  const unsigned nv_max = b->nv[T.cell_begin];
+  if (ncells <= 0 || ncells > cap_cells) return fail(DPM_ECAPACITY, "request exceeds slot cells");
+  if (!(L > 0.0f) || nsteps <= 0) return fail(DPM_EINVAL, "bad tissue parameters");
+  float l0max = 0.0f, a0max = 0.0f;
+  double rsum = 0.0;
+  for (int i = 0; i < ncells; ++i) {
+    if (nv[i] < 3 || nv[i] > nv_max) return fail(DPM_ECAPACITY, "request exceeds slot vertices");
+    if (!(a0[i] > 0.0f) || !(l0[i] > 0.0f) || !(r0[i] > 0.0f))
+      return fail(DPM_EINVAL, "a0, l0 and r0 must be positive");
+  }
+  // cell constants of the slot (active cells, then empty ones)
+  for (int i = 0; i < cap_cells; ++i) {
+    Cell2D &C = b->h_cells[T.cell_begin + i];
+    if (i < ncells) {
+      C.nv = nv[i];
+      C.a0 = a0[i];
+      C.l0 = l0[i];
+      C.kA = Ka[i] / std::sqrt(a0[i]);
+      C.kL = Kl[i] * std::sqrt(a0[i] / l0[i]);
+      C.Kb = Kb[i];
+      C.r0 = r0[i];
+      C.inv_l0 = 1.0f / l0[i];
+      C.inv_2r0 = 1.0f / (2.0f * r0[i]);
+      l0max = std::max(l0max, l0[i]);
+      a0max = std::max(a0max, a0[i]);
+      rsum += r0[i];
+    } else {
+      C.nv = 0;
+    }
+  }
+  T.L = L;
+  T.Kre = Kre;
+  T.Kat = Kat;
+  T.pbc = pbc ? 1 : 0;
+  T.l0max = l0max;
+  T.skin = (float)(b->skin_rel * 2.0 * rsum / ncells);
+  const double rad = std::sqrt(a0max / M_PI);
+  long cap = (long)std::floor(L / std::max(rad, 1e-6));
+  T.cap = (int)std::max(1L, std::min(cap, (long)kMaxBinsAxis));
+  T.cell_end = T.cell_begin + ncells;
+  T.steps_left = nsteps;
+  T.run_now = 0;
+  // positions into the slot's strided storage
+  std::vector<float2> stage((size_t)ncells * nv_max, make_float2(0.0f, 0.0f));
+  size_t off = 0;
+  for (int i = 0; i < ncells; ++i) {
+    for (unsigned v = 0; v < nv[i]; ++v)
+      stage[(size_t)i * nv_max + v] = make_float2(xy[2 * (off + v)], xy[2 * (off + v) + 1]);
+    off += nv[i];
+  }
+  cudaStream_t s = b->stream;
+  const uint32_t v0 = b->voff[T.cell_begin];
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells + T.cell_begin, b->h_cells.data() + T.cell_begin,
+                               sizeof(Cell2D) * cap_cells, cudaMemcpyHostToDevice, s));
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues + slot, &T, sizeof(Tissue2D), cudaMemcpyHostToDevice, s));
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_pos[b->cur] + v0, stage.data(), sizeof(float2) * stage.size(),
+                               cudaMemcpyHostToDevice, s));
+  DPM_CUDA_TRY(cudaMemsetAsync(b->d_force + v0, 0, sizeof(float2) * stage.size(), s));
+  DPM_CUDA_TRY(launch_geom2d(b->d_cells + T.cell_begin, b->d_pos[b->cur],
+                             b->d_geom[b->cur] + T.cell_begin, cap_cells, b->maxnv, s));
+  // the copies above read host memory that goes out of scope
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  return DPM_OK;
+}
+
+int pool2d_run(dpm2d_batch *b, int nsteps, float dt) {
+  const int R = b->rebuild_period;
+  if (nsteps % R) return fail(DPM_EINVAL, "pool chunks must be whole rebuild periods");
+  for (int i = 0; i < nsteps / R; ++i)
+    if (int r = b->run_block(R, dt, false)) return r;
+  return DPM_OK;
+}
+
+int pool2d_sync(dpm2d_batch *b) {
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DPM_OK;
+}
+
+int pool2d_fetch(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, float *xy, float *F) {
+  const Tissue2D &T = b->h_tissues[slot];
+  const unsigned nv_max = b->nv[T.cell_begin];
+  const uint32_t v0 = b->voff[T.cell_begin];
+  std::vector<float2> px((size_t)ncells * nv_max), pf((size_t)ncells * nv_max);
+  DPM_CUDA_TRY(cudaMemcpyAsync(px.data(), b->d_pos[b->cur] + v0, sizeof(float2) * px.size(),
+                               cudaMemcpyDeviceToHost, b->stream));
+  DPM_CUDA_TRY(cudaMemcpyAsync(pf.data(), b->d_force + v0, sizeof(float2) * pf.size(),
+                               cudaMemcpyDeviceToHost, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  size_t off = 0;
+  for (int i = 0; i < ncells; ++i) {
+    for (unsigned v = 0; v < nv[i]; ++v) {
+      const float2 p = px[(size_t)i * nv_max + v], f = pf[(size_t)i * nv_max + v];
+      xy[2 * (off + v)] = p.x;
+      xy[2 * (off + v) + 1] = p.y;
+      if (F) {
+        F[2 * (off + v)] = f.x;
+        F[2 * (off + v) + 1] = f.y;
+      }
+    }
+    off += nv[i];
+  }
+  return DPM_OK;
+}
+
+int pool2d_release(dpm2d_batch *b, int slot) {
+  Tissue2D &T = b->h_tissues[slot];
+  for (int c = T.cell_begin; c < T.cell_cap; ++c) b->h_cells[c].nv = 0;
+  T.cell_end = T.cell_begin;
+  T.steps_left = 0;
+  T.run_now = 0;
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells + T.cell_begin, b->h_cells.data() + T.cell_begin,
+                               sizeof(Cell2D) * (T.cell_cap - T.cell_begin),
+                               cudaMemcpyHostToDevice, b->stream));
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues + slot, &T, sizeof(Tissue2D), cudaMemcpyHostToDevice,
+                               b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DPM_OK;
+}
+
+} // namespace dpm

@@ -35,11 +35,14 @@ int ceil_log2l(long v) {
 
 struct dpm3d_batch {
   dpm_ctx *ctx = nullptr;
+  cudaStream_t stream = nullptr; // the context's, or the pool's own
+  bool own_stream = false;
   int ntissues = 0, ncells = 0, nv = 0, nf = 0;
   long nverts = 0;
   std::vector<Cell3D> h_cells;
   std::vector<Tissue3D> h_tissues;
   bool cells_set = false, tissues_set = false, uploaded = false, bend = false;
+  bool serving = false; // slot pool of a server: per-tissue step budgets
   DeviceArena arena;
   Mesh3D mesh{};
   Cell3D *d_cells = nullptr;
@@ -58,7 +61,13 @@ struct dpm3d_batch {
   float skin_rel = 0.1f;
   std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
 
-  ~dpm3d_batch() { clear_graphs(); }
+  ~dpm3d_batch() {
+    clear_graphs();
+    if (own_stream && stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+  }
 
   // skin = skin_rel * mean cell diameter of each tissue
   void update_skin() {
@@ -76,7 +85,7 @@ struct dpm3d_batch {
     graphs.clear();
   }
 
-  cudaError_t enqueue_rebuild(int g, cudaStream_t s) {
+  cudaError_t enqueue_rebuild(int g, int block_len, cudaStream_t s) {
     Rebuild3DArgs a{};
     a.cells = d_cells;
     a.tissues = d_tissues;
@@ -89,6 +98,7 @@ struct dpm3d_batch {
     a.stale = d_stale;
     a.ncells = ncells;
     a.ntissues = ntissues;
+    a.block_len = block_len;
     cudaError_t e = launch_binprep3d(a, local_bits, s);
     if (e != cudaSuccess) return e;
     bool alt = false;
@@ -100,7 +110,7 @@ struct dpm3d_batch {
     return launch_neighbors3d(a, local_bits, s);
   }
 
-  Step3DArgs step_args(int from, float dt, bool last) const {
+  Step3DArgs step_args(int from, float dt, bool last, int index) const {
     Step3DArgs a{};
     a.mesh = mesh;
     a.cells = d_cells;
@@ -111,10 +121,13 @@ struct dpm3d_batch {
     a.xout = d_pos[1 - from][0];
     a.yout = d_pos[1 - from][1];
     a.zout = d_pos[1 - from][2];
-    a.fx = last ? d_f[0] : nullptr;
-    a.fy = last ? d_f[1] : nullptr;
-    a.fz = last ? d_f[2] : nullptr;
-    a.wn_out = last ? d_wn : nullptr;
+    const bool out = serving || last;
+    a.fx = out ? d_f[0] : nullptr;
+    a.fy = out ? d_f[1] : nullptr;
+    a.fz = out ? d_f[2] : nullptr;
+    a.wn_out = out ? d_wn : nullptr;
+    a.all_forces = serving ? 0 : 1;
+    a.step_index = index;
     a.geom_in = d_geom[from];
     a.geom_out = d_geom[1 - from];
     a.geom0 = d_geom0;
@@ -129,11 +142,11 @@ struct dpm3d_batch {
   }
 
   cudaError_t enqueue_block(int len, int from, float dt, bool last, cudaStream_t s) {
-    cudaError_t e = enqueue_rebuild(from, s);
+    cudaError_t e = enqueue_rebuild(from, len, s);
     if (e != cudaSuccess) return e;
     int f = from;
     for (int i = 0; i < len; ++i) {
-      e = launch_step3d(step_args(f, dt, last && i == len - 1), s);
+      e = launch_step3d(step_args(f, dt, last && i == len - 1, i), s);
       if (e != cudaSuccess) return e;
       f = 1 - f;
     }
@@ -141,7 +154,7 @@ struct dpm3d_batch {
   }
 
   int run_block(int len, float dt, bool last) {
-    cudaStream_t s = ctx->stream;
+    cudaStream_t s = stream;
     uint32_t dtbits;
     std::memcpy(&dtbits, &dt, 4);
     auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0);
@@ -189,6 +202,7 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
   try {
     auto b = std::make_unique<dpm3d_batch>();
     b->ctx = ctx;
+    b->stream = ctx->stream;
     b->ntissues = ntissues;
     b->nv = nv;
     b->nf = nf;
@@ -247,9 +261,13 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
       T.cell_end = cb + ncells[t];
       T.cap = 1;
       T.nb = 1;
+      T.cell_cap = T.cell_end;
+      T.steps_left = kStepsUnlimited;
+      T.run_now = kStepsUnlimited;
       for (int c = cb; c < cb + ncells[t]; ++c) {
         std::memset(&b->h_cells[c], 0, sizeof(Cell3D));
         b->h_cells[c].tissue = (uint32_t)t;
+        b->h_cells[c].active = 1;
       }
       cb += ncells[t];
     }
@@ -315,7 +333,7 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
 int dpm3d_destroy(dpm3d_batch *b) {
   if (!b) return DPM_OK;
   cudaSetDevice(b->ctx->device);
-  cudaStreamSynchronize(b->ctx->stream);
+  cudaStreamSynchronize(b->stream);
   dpm_ctx *c = b->ctx;
   delete b;
   ctx_release(c);
@@ -356,12 +374,12 @@ int dpm3d_set_cells(dpm3d_batch *b, const float *Kv, const float *Ka, const floa
   b->bend = bend;
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells, b->h_cells.data(), sizeof(Cell3D) * b->ncells,
-                               cudaMemcpyHostToDevice, b->ctx->stream));
+                               cudaMemcpyHostToDevice, b->stream));
   if (b->tissues_set)
     DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
                                  sizeof(Tissue3D) * b->ntissues, cudaMemcpyHostToDevice,
-                                 b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                                 b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->cells_set = true;
   return DPM_OK;
 }
@@ -389,8 +407,8 @@ int dpm3d_set_tissues(dpm3d_batch *b, const float *L, const float *Kre, const in
   if (b->key_bits > 32) return fail(DPM_ECAPACITY, "cell-list keys exceed 32 bits");
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue3D) * b->ntissues,
-                               cudaMemcpyHostToDevice, b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                               cudaMemcpyHostToDevice, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->tissues_set = true;
   b->clear_graphs();
   return DPM_OK;
@@ -400,7 +418,7 @@ int dpm3d_upload(dpm3d_batch *b, const float *xyz) {
   if (int r = check3(b)) return r;
   if (!xyz) return fail(DPM_EINVAL, "null positions");
   cudaSetDevice(b->ctx->device);
-  cudaStream_t s = b->ctx->stream;
+  cudaStream_t s = b->stream;
   // de-interleave on the host into the structure-of-arrays layout
   const long V = b->nverts;
   std::vector<float> soa(3 * (size_t)V);
@@ -417,7 +435,7 @@ int dpm3d_upload(dpm3d_batch *b, const float *xyz) {
   DPM_CUDA_TRY(cudaMemsetAsync(b->d_wn, 0, V, s));
   DPM_CUDA_TRY(cudaMemsetAsync(b->d_err, 0, sizeof(int), s));
   DPM_CUDA_TRY(launch_geom3d(b->d_pos[0][0], b->d_pos[0][1], b->d_pos[0][2], b->mesh,
-                             b->d_geom[0], b->ncells, s));
+                             b->d_cells, b->d_geom[0], b->ncells, s));
   DPM_CUDA_TRY(cudaStreamSynchronize(s));
   b->uploaded = true;
   return DPM_OK;
@@ -444,7 +462,7 @@ int dpm3d_download(dpm3d_batch *b, float *xyz, float *F) {
   if (int r = check3(b)) return r;
   if (!b->uploaded) return fail(DPM_ESTATE, "nothing uploaded");
   cudaSetDevice(b->ctx->device);
-  cudaStream_t s = b->ctx->stream;
+  cudaStream_t s = b->stream;
   const long V = b->nverts;
   std::vector<float> soa(3 * (size_t)V);
   int err = 0;
@@ -480,8 +498,8 @@ int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts) {
   if (!counts) return fail(DPM_EINVAL, "null output");
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(counts, b->d_wn, b->nverts, cudaMemcpyDeviceToHost,
-                               b->ctx->stream));
-  DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                               b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DPM_OK;
 }
 
@@ -496,11 +514,184 @@ int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel) {
       cudaSetDevice(b->ctx->device);
       DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(),
                                    sizeof(Tissue3D) * b->ntissues, cudaMemcpyHostToDevice,
-                                   b->ctx->stream));
-      DPM_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+                                   b->stream));
+      DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
     }
   }
   return DPM_OK;
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Slot pools for the server
+// ---------------------------------------------------------------------------
+
+namespace dpm {
+
+int pool3d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv, int nf,
+                  const unsigned *faces, dpm3d_batch **out) {
+  if (nslots <= 0 || cells_per_slot <= 0) return fail(DPM_EINVAL, "empty pool");
+  std::vector<int> nc(nslots, cells_per_slot);
+  dpm3d_batch *b = nullptr;
+  if (int r = dpm3d_create(ctx, nslots, nc.data(), nv, nf, faces, &b)) return r;
+  b->serving = true;
+  for (auto &C : b->h_cells) C.active = 0;
+  for (auto &T : b->h_tissues) {
+    T.cell_cap = T.cell_end;
+    T.cell_end = T.cell_begin;
+    T.L = 1.0f;
+    T.cap = 1;
+    T.steps_left = 0;
+    T.run_now = 0;
+  }
+  // bins per axis are capped at 64, so local bin indices fit 18 bits
+  b->local_bits = 18;
+  b->key_bits = 18 + ceil_log2l(nslots);
+  if (b->key_bits > 32) {
+    dpm3d_destroy(b);
+    return fail(DPM_ECAPACITY, "too many slots for 32-bit cell-list keys");
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    b->stream = ctx->stream;
+    dpm3d_destroy(b);
+    return cuda_fail(e, "pool stream");
+  }
+  b->own_stream = true;
+  e = cudaMemcpyAsync(b->d_cells, b->h_cells.data(), sizeof(Cell3D) * b->ncells,
+                      cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue3D) * b->ntissues,
+                        cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) {
+    dpm3d_destroy(b);
+    return cuda_fail(e, "pool upload");
+  }
+  b->cells_set = b->tissues_set = b->uploaded = true;
+  *out = b;
+  return DPM_OK;
+}
+
+size_t pool3d_bytes(const dpm3d_batch *b) { return b->arena.capacity(); }
+
+int pool3d_assign(dpm3d_batch *b, int slot, int ncells, const float *Kv, const float *Ka,
+                  const float *Ks, const float *v0, const float *a0, const float *l0,
+                  const float *Kb, const float *adh, const float *xyz, float L, float Kre,
+                  int pbc, int nsteps) {
+  if (slot < 0 || slot >= b->ntissues) return fail(DPM_EINVAL, "no such slot");
+  Tissue3D &T = b->h_tissues[slot];
+  const int cap_cells = T.cell_cap - T.cell_begin;
+  if (ncells <= 0 || ncells > cap_cells) return fail(DPM_ECAPACITY, "request exceeds slot cells");
+  if (!(L > 0.0f) || nsteps <= 0) return fail(DPM_EINVAL, "bad tissue parameters");
+  bool bend = b->bend;
+  double vs = 0.0;
+  float v0max = 0.0f;
+  for (int i = 0; i < cap_cells; ++i) {
+    Cell3D &C = b->h_cells[T.cell_begin + i];
+    if (i < ncells) {
+      if (!(l0[i] > 0.0f) || !(v0[i] > 0.0f)) return fail(DPM_EINVAL, "v0 and l0 must be positive");
+      C.Kv = Kv[i];
+      C.Ka = Ka[i];
+      C.Ks = Ks[i];
+      C.v0 = v0[i];
+      C.a0 = a0[i];
+      C.l0 = l0[i];
+      C.Kb = Kb ? Kb[i] : 0.0f;
+      C.adh = adh ? adh[i] : l0[i] * 2.0f;
+      C.sa_scale = Ka[i] * std::sqrt(a0[i]) / l0[i] * 0.3f;
+      C.active = 1;
+      bend |= C.Kb != 0.0f;
+      vs += std::cbrt(v0[i]);
+      v0max = std::max(v0max, v0[i]);
+    } else {
+      C.active = 0;
+    }
+  }
+  if (bend != b->bend) {
+    b->bend = bend;
+    b->clear_graphs();
+  }
+  T.L = L;
+  T.Kre = Kre;
+  T.pbc = pbc ? 1 : 0;
+  T.skin = (float)(b->skin_rel * 2.0 * std::cbrt(3.0 / (4.0 * M_PI)) * vs / ncells);
+  const double rad = std::cbrt(3.0 * v0max / (4.0 * M_PI));
+  long cap = (long)std::floor(L / std::max(rad, 1e-6));
+  T.cap = (int)std::max(1L, std::min(cap, 64L));
+  T.cell_end = T.cell_begin + ncells;
+  T.steps_left = nsteps;
+  T.run_now = 0;
+  const size_t n = (size_t)ncells * b->nv, base = (size_t)T.cell_begin * b->nv;
+  std::vector<float> soa(3 * n);
+  for (size_t i = 0; i < n; ++i) {
+    soa[i] = xyz[3 * i];
+    soa[n + i] = xyz[3 * i + 1];
+    soa[2 * n + i] = xyz[3 * i + 2];
+  }
+  cudaStream_t s = b->stream;
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells + T.cell_begin, b->h_cells.data() + T.cell_begin,
+                               sizeof(Cell3D) * cap_cells, cudaMemcpyHostToDevice, s));
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues + slot, &T, sizeof(Tissue3D), cudaMemcpyHostToDevice, s));
+  for (int k = 0; k < 3; ++k) {
+    DPM_CUDA_TRY(cudaMemcpyAsync(b->d_pos[b->cur][k] + base, soa.data() + k * n,
+                                 sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    DPM_CUDA_TRY(cudaMemsetAsync(b->d_f[k] + base, 0, sizeof(float) * n, s));
+  }
+  DPM_CUDA_TRY(launch_geom3d(b->d_pos[b->cur][0] + base, b->d_pos[b->cur][1] + base,
+                             b->d_pos[b->cur][2] + base, b->mesh, b->d_cells + T.cell_begin,
+                             b->d_geom[b->cur] + T.cell_begin, cap_cells, s));
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  return DPM_OK;
+}
+
+int pool3d_run(dpm3d_batch *b, int nsteps, float dt) {
+  const int R = b->rebuild_period;
+  if (nsteps % R) return fail(DPM_EINVAL, "pool chunks must be whole rebuild periods");
+  for (int i = 0; i < nsteps / R; ++i)
+    if (int r = b->run_block(R, dt, false)) return r;
+  return DPM_OK;
+}
+
+int pool3d_sync(dpm3d_batch *b) {
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DPM_OK;
+}
+
+int pool3d_fetch(dpm3d_batch *b, int slot, int ncells, float *xyz, float *F) {
+  const Tissue3D &T = b->h_tissues[slot];
+  const size_t n = (size_t)ncells * b->nv, base = (size_t)T.cell_begin * b->nv;
+  std::vector<float> soa(3 * n), fs(3 * n);
+  for (int k = 0; k < 3; ++k) {
+    DPM_CUDA_TRY(cudaMemcpyAsync(soa.data() + k * n, b->d_pos[b->cur][k] + base,
+                                 sizeof(float) * n, cudaMemcpyDeviceToHost, b->stream));
+    DPM_CUDA_TRY(cudaMemcpyAsync(fs.data() + k * n, b->d_f[k] + base, sizeof(float) * n,
+                                 cudaMemcpyDeviceToHost, b->stream));
+  }
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      xyz[3 * i + k] = soa[k * n + i];
+      if (F) F[3 * i + k] = fs[k * n + i];
+    }
+  return DPM_OK;
+}
+
+int pool3d_release(dpm3d_batch *b, int slot) {
+  Tissue3D &T = b->h_tissues[slot];
+  for (int c = T.cell_begin; c < T.cell_cap; ++c) b->h_cells[c].active = 0;
+  T.cell_end = T.cell_begin;
+  T.steps_left = 0;
+  T.run_now = 0;
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_cells + T.cell_begin, b->h_cells.data() + T.cell_begin,
+                               sizeof(Cell3D) * (T.cell_cap - T.cell_begin),
+                               cudaMemcpyHostToDevice, b->stream));
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues + slot, &T, sizeof(Tissue3D), cudaMemcpyHostToDevice,
+                               b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DPM_OK;
+}
+
+} // namespace dpm
