@@ -214,15 +214,19 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel):
-    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+def profiled_traffic(summary):
+    """DRAM bytes (read + write) per launch from the committed ncu summary
+    `profiles/<summary>.md` (its "traffic (read + write) per launch" row)."""
+    p = os.path.join(ROOT, "profiles", summary + ".md")
     try:
         with open(p) as f:
-            d = json.load(f)
-        return d.get(kernel)
-    except (OSError, ValueError):
-        return None
+            for line in f:
+                if line.startswith("| traffic (read + write) per launch"):
+                    v, unit = line.split("|")[2].split()
+                    return float(v) * {"MB": 1e6, "GB": 1e9, "KB": 1e3}[unit]
+    except (OSError, ValueError, KeyError, IndexError):
+        pass
+    return None
 
 
 def launches_per_call(batch, sim_steps, period):
@@ -301,15 +305,18 @@ def run_ours(args, rank, world, local_rank):
     bytes_per_launch = 16.0 * V + 28.0 * N
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_per_launch / kern / 1e9
-    traffic = profiled_traffic("k2d_step_batched")
+    traffic = profiled_traffic("k2d_step_batched512")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS)",
                 "kernel": "k2d_step", "kernel_us": round(kern * 1e6, 2),
                 "bytes_per_launch": int(bytes_per_launch),
                 "traffic": None if traffic is None else int(traffic)}
 
-    # end to end through the C ABI: pinned host in, stepped, pinned host out
-    xy_pin = torch.from_numpy(np.ascontiguousarray(xy_host)).pin_memory()
+    # end to end through the C ABI: pinned host in, stepped, pinned host out;
+    # the input is the batch's current (relaxed) state, so the device work
+    # per step matches the timed region
+    xy_now, _ = b.download()
+    xy_pin = torch.from_numpy(np.ascontiguousarray(xy_now.reshape(-1))).pin_memory()
     out_pin = torch.empty_like(xy_pin).pin_memory()
     f_pin = torch.empty_like(xy_pin).pin_memory()
     e_iters = max(3, min(args.steps, 10))
@@ -346,9 +353,11 @@ def run_ours(args, rank, world, local_rank):
                          "calA0 ~ U[1.0,1.2], kb=0.01, packing fraction 0.6 (static box)",
              "tuning": ptuned}
 
+    p3 = plain3d(ctx, lambda n, fn: timed(None, n, fn), max(3, args.steps))
+
     served = None
     if args.serve_requests > 0:
-        served = run_served(ctx, value / world, args.serve_requests)
+        served = run_served(ctx, args.serve_requests)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -366,6 +375,7 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches_per_call(b, SIM_STEPS, tuned["rebuild_period"]) * args.steps,
         "roofline": roofline, "e2e": e2e, "plain": plain,
         "batched_over_plain": round(value / world / plain["value"], 2),
+        "plain3d": p3,
         "served": served,
         "clocks": clock_info,
     }
@@ -411,48 +421,78 @@ def served_requests(seed, nreq):
     return reqs
 
 
-def rate3d(ctx, level, steps=16):
-    """Vertex-steps/s of a 3D batch of 4 monolayers of 96 cells."""
-    import torch
+def plain3d(ctx, timed, iters, steps=16):
+    """The plain 3D monolayer: 256 icospheres at subdivision 3 (642 vertices,
+    1,280 faces), kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion range 0.1,
+    dt=0.002; `timed(iters, fn)` returns seconds for iters calls of fn."""
     from opencl_dpm_gb300 import clDPM
     from opencl_dpm_gb300.abi import Batch3D
-    rng = np.random.default_rng(5)
-    ts = [build_monolayer(clDPM, rng, 96, level) for _ in range(4)]
-    cat = lambda k: np.concatenate([t[k] for t in ts])
-    b = Batch3D(ctx, [96] * 4, ts[0]["faces"], ts[0]["nv"])
-    b.set_cells(cat("Kv"), cat("Ka"), cat("Ks"), cat("v0"), cat("a0"), cat("l0"), cat("Kb"),
-                cat("adh"))
-    b.set_tissues([t["L"] for t in ts], 1.0, 1)
-    b.upload(cat("xyz"))
-    b.step(steps, DT3)
-    ctx.synchronize()
-    t0 = time.perf_counter()
-    b.step(steps, DT3)
-    ctx.synchronize()
-    secs = time.perf_counter() - t0
-    torch.cuda.synchronize()
-    return b.nverts * steps / secs
+    t = build_monolayer(clDPM, np.random.default_rng(3), 256, 3)
+    b = Batch3D(ctx, [256], t["faces"], t["nv"])
+    b.set_cells(t["Kv"], t["Ka"], t["Ks"], t["v0"], t["a0"], t["l0"], t["Kb"], t["adh"])
+    b.set_tissues([t["L"]], 1.0, 1)
+    b.upload(t["xyz"])
+    for _ in range(3):
+        b.step(steps, DT3)
+    secs = timed(iters, lambda: b.step(steps, DT3))
+    return {"value": round(b.nverts * steps * iters / secs, 1), "unit": UNIT,
+            "ms_per_step": round(secs / iters * 1e3, 4), "sim_steps_per_step": steps,
+            "workload": "1 monolayer, 256 cells x 642 vertices (icosphere subdivision 3), "
+                        "jittered hexagonal lattice on z=0, kv=1 ka=0.5 ks=0.1 kb=0.05, "
+                        "adhesion 0.1, dt=0.002"}
 
 
-def run_served(ctx, rate2d, nreq, seed=77):
-    """Seeded Poisson arrivals at 80% of the device's measured capacity for
-    this request mix; latency = completion - arrival (host clock)."""
+def make_server(ctx):
+    from opencl_dpm_gb300 import clDPM
     from opencl_dpm_gb300.abi import Server
+    srv = Server(ctx, hbm_budget_bytes=32 << 30, chunk_steps=SERVE_CHUNK)
+    for slots, cells in POOLS_2D:
+        srv.add_pool2d(slots, cells, 32, DT)
+    for level in (2, 3):
+        proto = clDPM.Cell3D([0.0, 0.0, 0.0], 1.05, 1.0, level)
+        faces = np.asarray(proto.GetFaces(), np.uint32)
+        for slots, cells in POOLS_3D:
+            srv.add_pool3d(slots, cells, faces, int(proto.NV), DT3)
+    return srv
+
+
+def submit(srv, t, steps=None):
+    steps = t["steps"] if steps is None else steps
+    if t["dim"] == 2:
+        return srv.submit2d(t["nv"], t["Ka"], t["Kl"], t["Kb"], t["a0"], t["l0"], t["r0"],
+                            t["xy"], float(t["L"]), t["Kre"], t["Kat"], 1, steps, DT)
+    return srv.submit3d(t["nv"], t["Kv"], t["Ka"], t["Ks"], t["v0"], t["a0"], t["l0"],
+                        t["xyz"], float(t["L"]), t["Kre"], 1, steps, DT3, Kb=t["Kb"],
+                        adh=t["adh"])
+
+
+def served_capacity(ctx, seed, nreq=32, steps=2048):
+    """Vertex-steps/s of the server saturated with the same request mix (all
+    submitted at once, each for `steps` steps)."""
+    srv = make_server(ctx)
     reqs = served_requests(seed, nreq)
-    r3 = {lv: rate3d(ctx, lv) for lv in (2, 3)}
-    cost = [t["verts"] * t["steps"] / (rate2d if t["dim"] == 2 else r3[t["level"]]) for t in reqs]
-    lam = 0.8 / float(np.mean(cost))
+    for t in reqs:
+        submit(srv, t, steps)
+    t0 = time.perf_counter()
+    srv.drain()
+    secs = time.perf_counter() - t0
+    vs, _ = srv.stats()
+    srv.close()
+    return vs / secs
+
+
+def run_served(ctx, nreq, seed=77):
+    """Seeded Poisson arrivals at 80% of the server's measured capacity for
+    this request mix; latency = completion - arrival (host clock)."""
+    reqs = served_requests(seed, nreq)
+    cap = served_capacity(ctx, seed + 2)
+    mean_vs = float(np.mean([t["verts"] * t["steps"] for t in reqs]))
+    lam = 0.8 * cap / mean_vs
     rng = np.random.default_rng(seed + 1)
     arrival = np.cumsum(rng.exponential(1.0 / lam, size=nreq))
     arrival -= arrival[0]
 
-    srv = Server(ctx, hbm_budget_bytes=32 << 30, chunk_steps=SERVE_CHUNK)
-    for slots, cells in POOLS_2D:
-        srv.add_pool2d(slots, cells, 32, DT)
-    faces = {t["level"]: (t["faces"], t["nv"]) for t in reqs if t["dim"] == 3}
-    for lv, (f, nv) in sorted(faces.items()):
-        for slots, cells in POOLS_3D:
-            srv.add_pool3d(slots, cells, f, nv, DT3)
+    srv = make_server(ctx)
     pool_bytes = srv.pool_bytes()
 
     ids = [None] * nreq
@@ -464,15 +504,7 @@ def run_served(ctx, rate2d, nreq, seed=77):
     while nxt < nreq or running:
         now = time.perf_counter() - t0
         while nxt < nreq and arrival[nxt] <= now:
-            t = reqs[nxt]
-            if t["dim"] == 2:
-                ids[nxt] = srv.submit2d(t["nv"], t["Ka"], t["Kl"], t["Kb"], t["a0"], t["l0"],
-                                        t["r0"], t["xy"], float(t["L"]), t["Kre"], t["Kat"], 1,
-                                        t["steps"], DT)
-            else:
-                ids[nxt] = srv.submit3d(t["nv"], t["Kv"], t["Ka"], t["Ks"], t["v0"], t["a0"],
-                                        t["l0"], t["xyz"], float(t["L"]), t["Kre"], 1,
-                                        t["steps"], DT3, Kb=t["Kb"], adh=t["adh"])
+            ids[nxt] = submit(srv, reqs[nxt])
             running.add(nxt)
             nxt += 1
         if not running:
@@ -499,8 +531,9 @@ def run_served(ctx, rate2d, nreq, seed=77):
         "requests": nreq, "requests_2d": n2, "requests_3d": nreq - n2,
         "vertex_steps": vs, "makespan_s": round(makespan, 3), "rounds": rounds,
         "arrival_rate_per_s": round(lam, 3),
-        "load": "80% of capacity estimated from the measured batched 2D rate and 3D batch "
-                f"rates (level 2: {r3[2]:.3g}, level 3: {r3[3]:.3g} vertex-steps/s)",
+        "capacity": round(cap, 1),
+        "load": "arrival rate = 80% of the capacity measured first: the same server saturated "
+                "with 32 requests of this mix, 2,048 steps each",
         "pools": {"2d": [{"slots": s, "cells": c, "nv_max": 32} for s, c in POOLS_2D],
                   "3d": [{"slots": s, "cells": c} for s, c in POOLS_3D],
                   "bytes": pool_bytes, "chunk_steps": SERVE_CHUNK},

@@ -113,6 +113,10 @@ int dpm2d_sizes(dpm2d_batch *b, int *ncells, long *nvertices);
  * in steps (even) and skin distance relative to the mean cell radius. */
 int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel,
                      int warps_per_block);
+/* Step-kernel variant 0..3 (bit 0: registers capped for 32 resident warps
+ * per SM; bit 1: dynamic schedule).  Every variant gives identical results;
+ * dpm2d_autotune picks the fastest. */
+int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant);
 
 /* Diagnostics: per-vertex containment flags of the last step (uint8 per
  * vertex; 1 = inside another cell, the reference's `overlaps`), per-cell
@@ -136,9 +140,11 @@ int dpm2d_bins(dpm2d_batch *b, int *local_bits, int *nbins, float *binw,
  * synchronizing.  For per-kernel timing and profiling. */
 int dpm2d_step_kernel(dpm2d_batch *b, float dt);
 
-/* Autotuner: times warps per block (4, 8, 16) x register/occupancy variant
- * (0: compiler's choice, 1: 32 resident warps per SM) x (rebuild period,
- * skin) on this batch's current state, restores the state, and applies the
+/* Autotuner: times warps per block (4, 8, 16) x step-kernel variant (bit 0:
+ * registers capped for 32 resident warps per SM, else the compiler's choice;
+ * bit 1: dynamic schedule, resident warps taking cells from a counter, else
+ * one warp per cell in launch order) x (rebuild period, skin) on this
+ * batch's current state, restores the state, and applies the
  * fastest.  Choices are cached as JSON lines keyed by the batch's shape in
  * $DPM_TUNE_CACHE (default ~/.cache/dpm_gb300_tune2d.jsonl); with use_cache
  * a cached choice is applied without trials.  Allocates a temporary copy of
@@ -249,9 +255,16 @@ int dpm_serve_submit3d(dpm_server *s, int ncells, int nv, const float *Kv,
                        const float *a0, const float *l0, const float *Kb,
                        const float *adh, const float *xyz, float L, float Kre,
                        int pbc, int nsteps, float dt, uint64_t *id);
-/* One round: admit, step every pool by chunk_steps, retire finished
- * requests.  Counts after the round are returned (any pointer may be NULL). */
+/* Advances the server: every pool runs chunks of chunk_steps on its own
+ * stream, independently of the others.  Returns once at least one pool has
+ * completed a chunk (its finished requests read back, waiting requests
+ * admitted into it, its next chunk enqueued), or at once when nothing is in
+ * flight.  Counts afterwards are returned (any pointer may be NULL);
+ * `finished` counts the requests completed by this call.  A wait longer than
+ * 300 s fails with DPM_ECUDA. */
 int dpm_serve_step(dpm_server *s, int *active, int *waiting, int *finished);
+/* Calls dpm_serve_step until nothing is running or waiting. */
+int dpm_serve_drain(dpm_server *s);
 /* status: 0 waiting, 1 running, 2 done.  When done, copies the final
  * positions and the forces of the request's last step, and the time from
  * submit to completion. */

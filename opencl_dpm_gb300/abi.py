@@ -40,6 +40,7 @@ SIGNATURES = {
     "dpm2d_download": (ctypes.c_int, [_vp, _vp, _vp]),
     "dpm2d_sizes": (ctypes.c_int, [_vp, _c_int_p, _c_long_p]),
     "dpm2d_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float, ctypes.c_int]),
+    "dpm2d_set_kernel_variant": (ctypes.c_int, [_vp, ctypes.c_int]),
     "dpm2d_last_contained": (ctypes.c_int, [_vp, _c_ubyte_p]),
     "dpm2d_cell_areas": (ctypes.c_int, [_vp, _c_float_p]),
     "dpm2d_stats": (ctypes.c_int, [_vp, _c_long_p, _c_long_p]),
@@ -78,6 +79,7 @@ SIGNATURES = {
                            [ctypes.c_float] * 2 + [ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                    ctypes.POINTER(ctypes.c_uint64)]),
     "dpm_serve_step": (ctypes.c_int, [_vp, _c_int_p, _c_int_p, _c_int_p]),
+    "dpm_serve_drain": (ctypes.c_int, [_vp]),
     "dpm_serve_result": (ctypes.c_int, [_vp, ctypes.c_uint64, _c_float_p, _c_float_p,
                                         ctypes.POINTER(ctypes.c_double), _c_int_p]),
     "dpm_serve_forget": (ctypes.c_int, [_vp, ctypes.c_uint64]),
@@ -198,6 +200,9 @@ class Batch2D:
 
     def set_tuning(self, rebuild_period=0, skin_rel=0.0, warps=0):
         check(self.lib.dpm2d_set_tuning(self.h, rebuild_period, skin_rel, warps))
+
+    def set_kernel_variant(self, variant: int):
+        check(self.lib.dpm2d_set_kernel_variant(self.h, variant))
 
     def upload(self, xy):
         xy = _f32(xy)
@@ -402,10 +407,14 @@ class Server:
         return rid.value
 
     def step(self):
-        """One round; returns (active, waiting, finished)."""
+        """Advances until some pool completes a chunk; returns (active,
+        waiting, finished by this call)."""
         a, w, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self.lib.dpm_serve_step(self.h, ctypes.byref(a), ctypes.byref(w), ctypes.byref(f)))
         return a.value, w.value, f.value
+
+    def drain(self):
+        check(self.lib.dpm_serve_drain(self.h))
 
     def status(self, rid: int) -> int:
         st = ctypes.c_int()

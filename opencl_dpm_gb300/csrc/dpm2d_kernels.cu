@@ -408,18 +408,12 @@ template <int S, int W, int OCC> struct StepOcc {
       OCC == 0 ? 1 : (kThreads / (W * 32) > 0 ? kThreads / (W * 32) : 1);
 };
 
-template <int S, int W, int OCC>
-__global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
-    k2d_step(Step2DArgs a) {
-  constexpr int M = 32 * S;
-  __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
-  __shared__ unsigned char sh_f[W][M];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * W + w;
-  if (c >= a.ncells) return;
-  float *sx = sh_x[w], *sy = sh_y[w], *nxs = sh_nx[w], *nys = sh_ny[w];
-  unsigned char *sf = sh_f[w];
-
+// One step of cell c by one warp; (sx, sy), (nxs, nys) and sf are the warp's
+// shared-memory ring, neighbour ring and containment flags (32*S entries).
+template <int S>
+__device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, const int lane,
+                                          float *sx, float *sy, float *nxs, float *nys,
+                                          unsigned char *sf) {
   const Cell2D cp = a.cells[c];
   const int n = (int)cp.nv;
   if (n == 0) return;  // an empty slot
@@ -712,24 +706,87 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
   }
 }
 
+// Static schedule: warp w of block b takes cell b*W + w.
 template <int S, int W, int OCC>
-cudaError_t launch_step_sw(const Step2DArgs &a, cudaStream_t s) {
+__global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
+    k2d_step(Step2DArgs a) {
+  constexpr int M = 32 * S;
+  __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
+  __shared__ unsigned char sh_f[W][M];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * W + w;
+  if (c >= a.ncells) return;
+  step_cell<S>(a, c, lane, sh_x[w], sh_y[w], sh_nx[w], sh_ny[w], sh_f[w]);
+}
+
+// Dynamic schedule: a grid of exactly the resident blocks whose warps take
+// the next cell from a counter until none is left.  The work per cell varies
+// with its neighbours, so no warp idles while cells remain and no block is
+// held resident by one slow warp.  The last warp to finish resets the two
+// counters (next cell, finished warps) for the next launch.
+template <int S, int W, int OCC>
+__global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
+    k2d_step_dyn(Step2DArgs a) {
+  constexpr int M = 32 * S;
+  __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
+  __shared__ unsigned char sh_f[W][M];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = atomicAdd(a.sched, 1);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= a.ncells) break;
+    step_cell<S>(a, c, lane, sh_x[w], sh_y[w], sh_nx[w], sh_ny[w], sh_f[w]);
+    __syncwarp();
+  }
+  if (lane == 0) {
+    const int warps = (int)gridDim.x * W;
+    if (atomicAdd(a.sched + 1, 1) == warps - 1) {
+      atomicExch(a.sched, 0);
+      atomicExch(a.sched + 1, 0);
+    }
+  }
+}
+
+template <int S, int W, int OCC>
+cudaError_t launch_step_sw(const Step2DArgs &a, bool dyn, cudaStream_t s) {
+  if (dyn && a.sched) {
+    // resident blocks per SM of this variant, and the device's SM count
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, k2d_step_dyn<S, W, OCC>, W * 32, 0);
+      if (e != cudaSuccess) return e;
+      int dev = 0;
+      e = cudaGetDevice(&dev);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) per_sm = 1;
+    }
+    const int need = (a.ncells + W - 1) / W;
+    const int grid = need < per_sm * sms ? need : per_sm * sms;
+    k2d_step_dyn<S, W, OCC><<<grid, W * 32, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   const int grid = (a.ncells + W - 1) / W;
   k2d_step<S, W, OCC><<<grid, W * 32, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int S, int OCC>
-cudaError_t launch_step_so(const Step2DArgs &a, int warps, cudaStream_t s) {
+cudaError_t launch_step_so(const Step2DArgs &a, int warps, bool dyn, cudaStream_t s) {
   // 16 warps of 8 slots would exceed the static shared-memory limit
-  if (warps == 4) return launch_step_sw<S, 4, OCC>(a, s);
-  if (warps == 16 && S <= 4) return launch_step_sw<S, (S <= 4 ? 16 : 8), OCC>(a, s);
-  return launch_step_sw<S, 8, OCC>(a, s);
+  if (warps == 4) return launch_step_sw<S, 4, OCC>(a, dyn, s);
+  if (warps == 16 && S <= 4) return launch_step_sw<S, (S <= 4 ? 16 : 8), OCC>(a, dyn, s);
+  return launch_step_sw<S, 8, OCC>(a, dyn, s);
 }
 
+// variant bit 0: register cap for occupancy; bit 1: dynamic schedule
 template <int S>
-cudaError_t launch_step_s(const Step2DArgs &a, int warps, int occ, cudaStream_t s) {
-  return occ ? launch_step_so<S, 1>(a, warps, s) : launch_step_so<S, 0>(a, warps, s);
+cudaError_t launch_step_s(const Step2DArgs &a, int warps, int variant, cudaStream_t s) {
+  const bool dyn = (variant & 2) != 0;
+  return (variant & 1) ? launch_step_so<S, 1>(a, warps, dyn, s)
+                       : launch_step_so<S, 0>(a, warps, dyn, s);
 }
 
 } // namespace

@@ -24,6 +24,7 @@ struct Step2DArgs {
   int step_index;  // index of this step within its rebuild period
   int all_forces;  // 1: force_out/flags_out take every cell's values; 0: only
                    // those of tissues whose step budget ends at this step
+  int *sched;      // two zeroed counters for the dynamic schedule, or nullptr
 };
 
 struct Rebuild2DArgs {
@@ -50,9 +51,10 @@ cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom,
 cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
 // Neighbour lists from the sorted cell list (one warp per cell).
 cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
-// One fused time step.  warps: 4, 8 or 16 per block; occ: 1 caps registers
-// for 32 resident warps per SM, 0 lets the compiler choose.
-cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int occ,
+// One fused time step.  warps: 4, 8 or 16 per block; variant bit 0 caps
+// registers for 32 resident warps per SM (else the compiler chooses), bit 1
+// selects the dynamic schedule (needs a.sched).
+cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int variant,
                           cudaStream_t s);
 
 // Host mirror of the bin arithmetic (for the host rebuild check).

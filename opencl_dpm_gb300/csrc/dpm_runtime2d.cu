@@ -88,6 +88,7 @@ struct dpm2d_batch {
   Geom2D *d_geom[2] = {nullptr, nullptr};
   Geom2D *d_geom0 = nullptr;
   int *d_nn = nullptr, *d_nbr = nullptr, *d_stale = nullptr, *d_err = nullptr;
+  int *d_sched = nullptr; // dynamic-schedule counters of the step kernel
   uint32_t *d_keys = nullptr, *d_vals = nullptr, *d_keys_alt = nullptr, *d_vals_alt = nullptr;
   uint32_t *d_sort_scratch = nullptr;
   int cur = 0;
@@ -175,6 +176,7 @@ struct dpm2d_batch {
     a.nbr = d_nbr;
     a.stale = d_stale;
     a.err = d_err;
+    a.sched = d_sched;
     a.ncells = ncells;
     a.dt = dt;
     return a;
@@ -355,6 +357,7 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     b->d_nbr = A.take<int>(N * kMaxNB2D);
     b->d_stale = A.take<int>(ntissues);
     b->d_err = A.take<int>(1);
+    b->d_sched = A.take<int>(2);
     b->d_keys = A.take<uint32_t>(N);
     b->d_vals = A.take<uint32_t>(N);
     b->d_keys_alt = A.take<uint32_t>(N);
@@ -493,6 +496,14 @@ int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel, int war
       DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
     }
   }
+  return DPM_OK;
+}
+
+int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant) {
+  if (int r = check_batch(b)) return r;
+  if (variant < 0 || variant > 3) return fail(DPM_EINVAL, "step-kernel variant must be 0..3");
+  b->occ = variant;
+  b->clear_graphs();
   return DPM_OK;
 }
 
@@ -649,7 +660,8 @@ std::string tune_key(const dpm2d_batch *b, int sm_count) {
     return k;
   };
   char buf[160];
-  std::snprintf(buf, sizeof(buf), "2d sm%d t%d c%d v%d nv%d", sm_count, bucket(b->ntissues),
+  // "k2": step-kernel variants 0..3 (register cap x dynamic schedule)
+  std::snprintf(buf, sizeof(buf), "2d k2 sm%d t%d c%d v%d nv%d", sm_count, bucket(b->ntissues),
                 bucket(b->ncells), bucket(b->nverts), b->maxnv);
   return buf;
 }
@@ -751,7 +763,7 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache, in
     const float skins[3] = {0.08f, 0.15f, 0.3f};
     int rc = DPM_OK;
     for (int wi = 0; wi < 3 && rc == DPM_OK; ++wi)
-      for (int oi = 0; oi < 2 && rc == DPM_OK; ++oi)
+      for (int oi = 0; oi < 4 && rc == DPM_OK; ++oi)
         for (int pi = 0; pi < 3 && rc == DPM_OK; ++pi) {
           if (warps_set[wi] == 16 && b->maxnv > 128) continue;
           if ((rc = apply(warps_set[wi], oi, periods[pi], skins[pi]))) break;
@@ -873,6 +885,7 @@ int pool2d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv_max, dpm2
 }
 
 size_t pool2d_bytes(const dpm2d_batch *b) { return b->arena.capacity(); }
+cudaStream_t pool2d_stream(const dpm2d_batch *b) { return b->stream; }
 
 int pool2d_assign(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, const float *Ka,
                   const float *Kl, const float *Kb, const float *a0, const float *l0,

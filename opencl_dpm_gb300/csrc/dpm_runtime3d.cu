@@ -576,6 +576,7 @@ int pool3d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv, int nf,
 }
 
 size_t pool3d_bytes(const dpm3d_batch *b) { return b->arena.capacity(); }
+cudaStream_t pool3d_stream(const dpm3d_batch *b) { return b->stream; }
 
 int pool3d_assign(dpm3d_batch *b, int slot, int ncells, const float *Kv, const float *Ka,
                   const float *Ks, const float *v0, const float *a0, const float *l0,

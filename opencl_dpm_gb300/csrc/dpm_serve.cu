@@ -2,18 +2,21 @@
 //
 // A server owns slot pools (dpm_runtime.hpp): 2D pools keyed by cells per
 // slot, vertices per cell and time step; 3D pools keyed by mesh and time
-// step.  Each round of dpm_serve_step
-//   1. admits waiting requests, oldest first, into the smallest pool whose
-//      slots fit them, while a slot is free and the resident footprint of
-//      admitted requests stays within the HBM budget (a request that does
-//      not fit yet does not block smaller ones behind it);
-//   2. enqueues one chunk of steps on every pool with work, each on its own
-//      stream, so 2D and 3D pools run concurrently; inside a pool every
-//      tissue spends its own step budget and then stays frozen;
-//   3. waits for the pools, reads back every request whose budget ran out,
-//      frees its slot and stamps its completion time.
-// Requests admitted in a later round join the running pools between
-// chunks; a request's arithmetic does not depend on what shares its pool.
+// step.  Every pool advances on its own stream, one chunk of steps at a
+// time, independently of the others.  Whenever a pool's chunk completes,
+// dpm_serve_step
+//   1. reads back every request of that pool whose step budget ran out,
+//      frees its slot and stamps its completion time;
+//   2. admits waiting requests, oldest first, into the smallest idle pool
+//      whose slots fit them, while a slot is free and the resident
+//      footprint of admitted requests stays within the HBM budget (a
+//      request that does not fit yet does not block smaller ones behind
+//      it);
+//   3. enqueues the pool's next chunk; inside a pool every tissue spends its
+//      own step budget and then stays frozen.
+// So 2D and 3D pools overlap on the device, a slow pool does not hold back
+// a fast one, and requests join a running pool between its chunks.  A
+// request's arithmetic does not depend on what shares its pool.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,6 +26,7 @@
 #include <map>
 #include <memory>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "dpm_common.cuh"
@@ -65,7 +69,12 @@ struct Pool {
   dpm3d_batch *b3 = nullptr;
   std::vector<Request *> slots;
   int active = 0;
+  bool busy = false;         // a chunk is in flight
+  cudaEvent_t done = nullptr; // recorded after each chunk
 };
+
+// Longest wait for any pool's chunk before dpm_serve_step gives up.
+constexpr double kPoolWaitLimitS = 300.0;
 
 } // namespace
 
@@ -77,12 +86,12 @@ struct dpm_server {
   std::vector<Pool> pools;
   std::deque<Request *> waiting;
   std::map<uint64_t, std::unique_ptr<Request>> all;
-  long steps_done = 0;
   double vertex_steps = 0.0;
   ~dpm_server() {
     for (auto &p : pools) {
       if (p.b2) dpm2d_destroy(p.b2);
       if (p.b3) dpm3d_destroy(p.b3);
+      if (p.done) cudaEventDestroy(p.done);
     }
   }
 };
@@ -124,7 +133,7 @@ int admit(dpm_server *s) {
     int best = -1, slot = -1;
     for (int p = 0; p < (int)s->pools.size(); ++p) {
       Pool &P = s->pools[p];
-      if (!fits(P, *r)) continue;
+      if (P.busy || !fits(P, *r)) continue;
       auto fs = std::find(P.slots.begin(), P.slots.end(), nullptr);
       if (fs == P.slots.end()) continue;
       const bool smaller = best < 0 || P.cells_per_slot < s->pools[best].cells_per_slot ||
@@ -161,6 +170,36 @@ int admit(dpm_server *s) {
     r->t_admit = now_s();
     s->resident += r->footprint;
     it = s->waiting.erase(it);
+  }
+  return DPM_OK;
+}
+
+// Accounts one completed chunk of pool P: every request's budget shrinks by
+// the chunk; requests whose budget ran out are read back and their slots
+// freed.
+int retire(dpm_server *s, Pool &P, int *nfin) {
+  for (int slot = 0; slot < (int)P.slots.size(); ++slot) {
+    Request *r = P.slots[slot];
+    if (!r) continue;
+    const int done = std::min(r->remaining, s->chunk);
+    r->remaining -= done;
+    s->vertex_steps += (double)done * (r->dim == 2 ? r->x.size() / 2 : r->x.size() / 3);
+    if (r->remaining > 0) continue;
+    int rc;
+    if (P.b2) {
+      rc = pool2d_fetch(P.b2, slot, r->ncells, r->nv.data(), r->x.data(), r->f.data());
+      if (!rc) rc = pool2d_release(P.b2, slot);
+    } else {
+      rc = pool3d_fetch(P.b3, slot, r->ncells, r->x.data(), r->f.data());
+      if (!rc) rc = pool3d_release(P.b3, slot);
+    }
+    if (rc) return rc;
+    r->status = 2;
+    r->t_done = now_s();
+    P.slots[slot] = nullptr;
+    P.active--;
+    s->resident -= r->footprint;
+    ++*nfin;
   }
   return DPM_OK;
 }
@@ -202,6 +241,10 @@ int dpm_serve_add_pool2d(dpm_server *s, int slots, int cells_per_slot, int nv_ma
     dpm2d_destroy(P.b2);
     return fail(DPM_EINVAL, "chunk_steps must be a multiple of 16 for 2D pools");
   }
+  if (cudaError_t e = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) {
+    dpm2d_destroy(P.b2);
+    return cuda_fail(e, "pool event");
+  }
   P.slots.assign(slots, nullptr);
   s->pools.push_back(std::move(P));
   return DPM_OK;
@@ -221,6 +264,10 @@ int dpm_serve_add_pool3d(dpm_server *s, int slots, int cells_per_slot, int nv, i
   if (s->chunk % 8) {
     dpm3d_destroy(P.b3);
     return fail(DPM_EINVAL, "chunk_steps must be a multiple of 8 for 3D pools");
+  }
+  if (cudaError_t e = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) {
+    dpm3d_destroy(P.b3);
+    return cuda_fail(e, "pool event");
   }
   P.slots.assign(slots, nullptr);
   s->pools.push_back(std::move(P));
@@ -317,43 +364,38 @@ int dpm_serve_submit3d(dpm_server *s, int ncells, int nv, const float *Kv, const
 int dpm_serve_step(dpm_server *s, int *active, int *waiting, int *finished) {
   if (!s) return fail(DPM_EINVAL, "null server");
   cudaSetDevice(s->ctx->device);
-  if (int r = admit(s)) return r;
-  // one chunk on every pool with work, each on its own stream
-  for (auto &P : s->pools) {
-    if (!P.active) continue;
-    const int rc = P.b2 ? pool2d_run(P.b2, s->chunk, P.dt) : pool3d_run(P.b3, s->chunk, P.dt);
-    if (rc) return rc;
-  }
   int nfin = 0;
-  for (int p = 0; p < (int)s->pools.size(); ++p) {
-    Pool &P = s->pools[p];
-    if (!P.active) continue;
-    if (int r = P.b2 ? pool2d_sync(P.b2) : pool3d_sync(P.b3)) return r;
-    for (int slot = 0; slot < (int)P.slots.size(); ++slot) {
-      Request *r = P.slots[slot];
-      if (!r) continue;
-      const int done = std::min(r->remaining, s->chunk);
-      r->remaining -= done;
-      s->vertex_steps += (double)done * (r->dim == 2 ? r->x.size() / 2 : r->x.size() / 3);
-      if (r->remaining > 0) continue;
-      int rc;
-      if (P.b2) {
-        rc = pool2d_fetch(P.b2, slot, r->ncells, r->nv.data(), r->x.data(), r->f.data());
-        if (!rc) rc = pool2d_release(P.b2, slot);
-      } else {
-        rc = pool3d_fetch(P.b3, slot, r->ncells, r->x.data(), r->f.data());
-        if (!rc) rc = pool3d_release(P.b3, slot);
-      }
-      if (rc) return rc;
-      r->status = 2;
-      r->t_done = now_s();
-      P.slots[slot] = nullptr;
-      P.active--;
-      s->resident -= r->footprint;
-      ++nfin;
+  const double deadline = now_s() + kPoolWaitLimitS;
+  for (;;) {
+    // pools whose chunk completed
+    int progressed = 0;
+    for (auto &P : s->pools) {
+      if (!P.busy) continue;
+      const cudaError_t e = cudaEventQuery(P.done);
+      if (e == cudaErrorNotReady) continue;
+      if (e != cudaSuccess) return cuda_fail(e, "pool chunk");
+      P.busy = false;
+      ++progressed;
+      if (int r = retire(s, P, &nfin)) return r;
     }
+    if (int r = admit(s)) return r;
+    // next chunk on every idle pool with work, each on its own stream
+    int inflight = 0;
+    for (auto &P : s->pools) {
+      if (!P.busy && P.active) {
+        const int rc =
+            P.b2 ? pool2d_run(P.b2, s->chunk, P.dt) : pool3d_run(P.b3, s->chunk, P.dt);
+        if (rc) return rc;
+        const cudaStream_t st = P.b2 ? pool2d_stream(P.b2) : pool3d_stream(P.b3);
+        if (cudaError_t e = cudaEventRecord(P.done, st)) return cuda_fail(e, "pool event");
+        P.busy = true;
+      }
+      inflight += P.busy ? 1 : 0;
+    }
+    if (progressed || !inflight) break;
+    if (now_s() > deadline) return fail(DPM_ECUDA, "timed out waiting for a pool's chunk");
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
-  s->steps_done += s->chunk;
   if (active) {
     int a = 0;
     for (auto &P : s->pools) a += P.active;
@@ -361,6 +403,15 @@ int dpm_serve_step(dpm_server *s, int *active, int *waiting, int *finished) {
   }
   if (waiting) *waiting = (int)s->waiting.size();
   if (finished) *finished = nfin;
+  return DPM_OK;
+}
+
+int dpm_serve_drain(dpm_server *s) {
+  if (!s) return fail(DPM_EINVAL, "null server");
+  int a = 0, w = 0;
+  do {
+    if (int r = dpm_serve_step(s, &a, &w, nullptr)) return r;
+  } while (a || w);
   return DPM_OK;
 }
 
@@ -377,7 +428,6 @@ int dpm_serve_result(dpm_server *s, uint64_t id, float *x, float *F, double *lat
   if (latency_s) *latency_s = r.t_done - r.t_submit;
   return DPM_OK;
 }
-
 int dpm_serve_forget(dpm_server *s, uint64_t id) {
   if (!s) return fail(DPM_EINVAL, "null server");
   auto it = s->all.find(id);

@@ -202,3 +202,23 @@ def test_cell_list_bit_exact(ctx):
     for c in range(len(nn)):
         if nn[c] > 0:
             assert np.array_equal(hnbr[c, :nn[c]], nbr[c, :nn[c]])
+
+
+def test_kernel_variants_identical(ctx):
+    """Register cap and static/dynamic schedule change nothing in the results
+    (the dynamic schedule's counters reset themselves between launches)."""
+    rng = np.random.default_rng(31)
+    states = [make_tissue2d(int(rng.integers(8, 60)), int(rng.choice([16, 32, 48])),
+                            phi=float(rng.uniform(0.6, 0.9)), Kb=0.01, seed=200 + t)
+              for t in range(5)]
+    out = {}
+    for variant in range(4):
+        for warps in (4, 8, 16):
+            b = gpu_batch2d(ctx, states, dict(warps=warps))
+            b.set_kernel_variant(variant)
+            b.step(40, DT)
+            b.step(7, DT)
+            out[(variant, warps)] = b.download()
+    ref = out[(1, 8)]
+    for k, (xy, F) in out.items():
+        assert np.array_equal(xy, ref[0]) and np.array_equal(F, ref[1]), k

@@ -84,7 +84,8 @@ def test_serve_2d_mix_equals_alone(ctx):
     ids = [submit2d(srv, s, n) for s, n in reqs]
     trace = drain(srv, ids)
     # five slots, seven requests: some waited and joined later
-    assert trace[0][1] == 2 and max(a for a, _, _ in trace) <= 5
+    assert sum(trace[0]) == 7 and trace[0][1] + trace[0][2] >= 2
+    assert max(a for a, _, _ in trace) <= 5
     for rid, (s, n) in zip(ids, reqs):
         x, F, lat = srv.result(rid)
         ax, aF = alone2d(ctx, s, n)
