@@ -192,7 +192,8 @@ int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *Ka,
 
 /* Creates a batch of 3D tissues whose cells all share the mesh topology
  * faces[nf*3] over nv vertices (the reference uses cell 0's face table for
- * every cell, src/Tissue3D.cpp:144-146).  nv <= 2562. */
+ * every cell, src/Tissue3D.cpp:144-146).  nv <= 642 (icosphere subdivision
+ * 3). */
 int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv,
                  int nf, const unsigned *faces, dpm3d_batch **out);
 int dpm3d_destroy(dpm3d_batch *b);

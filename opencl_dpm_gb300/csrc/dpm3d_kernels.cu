@@ -118,11 +118,15 @@ __device__ __forceinline__ float winding_reach(const Geom3D &g) {
   return g.R + 1.05f * g.emax;
 }
 
+// Per-warp bit mask of a neighbour's vertices near the point under test.
+constexpr int kNearWords = (kMaxNV3D + 31) / 32;
+
 // Shared-memory layout of k3d_step (see step3d_smem_bytes).
 struct Smem3D {
-  float *px, *py, *pz, *fx, *fy, *fz, *qx, *qy, *qz, *ux, *uy, *uz, *red;
+  float *px, *py, *pz, *fx, *fy, *fz, *qx, *qy, *qz, *red;
   float *bnx, *bny, *bnz, *bnl, *bgx, *bgy, *bgz;
   int *ncand;
+  unsigned *near;
   uint16_t *faces, *cand;
   unsigned char *wnc;
 };
@@ -139,10 +143,9 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   s.qx = f; f += nv;
   s.qy = f; f += nv;
   s.qz = f; f += nv;
-  s.ux = f; f += kWarps * nv;
-  s.uy = f; f += kWarps * nv;
-  s.uz = f; f += kWarps * nv;
   s.red = f; f += 64;
+  s.near = reinterpret_cast<unsigned *>(f);
+  f += kWarps * kNearWords;
   if (bend) {
     s.bnx = f; f += nf;
     s.bny = f; f += nf;
@@ -166,6 +169,103 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
 }
 
 __device__ __forceinline__ f3 vtx(const Smem3D &s, int i) { return mk(s.px[i], s.py[i], s.pz[i]); }
+__device__ __forceinline__ f3 nbv(const Smem3D &s, int i) { return mk(s.qx[i], s.qy[i], s.qz[i]); }
+
+// One face term of the reference's winding sum (Cell3D_Kernel.cl:281-297):
+// unit vectors from the point to the corners, the denominator of the
+// triangle's half solid angle, and its numerator.
+__device__ __forceinline__ void face_term(const Smem3D &s, int i0, int i1, int i2, f3 pt,
+                                          float &num, float &denom) {
+  const f3 u = normalize(nbv(s, i0) - pt), vv = normalize(nbv(s, i1) - pt),
+           ww = normalize(nbv(s, i2) - pt);
+  denom = 1.0f + dot(u, vv) + dot(vv, ww) + dot(ww, u);
+  num = dot(u, cross(vv, ww));
+}
+
+__device__ __forceinline__ bool near_bit(const unsigned *m, int i) {
+  return (m[i >> 5] >> (i & 31)) & 1u;
+}
+
+// The reference's winding number of point pt with respect to the staged
+// neighbour mesh (s.q*), as the sum over its faces of 2 atan2(num, denom) /
+// 4 pi, leaving out faces with denom < 1e-8.  One warp; every lane returns
+// the value.
+//
+// Over a closed mesh the full sum is 4 pi times the topological winding
+// number, 0 for a point outside.  A face's term can be dropped (its solid
+// angle is at least ~pi) only from within 1.155 r of the centre of its
+// smallest enclosing circle (radius r <= longest edge / sqrt 3), i.e. within
+// 1.25 x the mesh's longest edge of each of its corners.  So when a plane
+// separates pt from every neighbour vertex (pt outside the convex hull), the
+// reference's sum equals minus the sum of the dropped terms, up to the
+// rounding of the reference's own summation: only faces with a corner near
+// pt are evaluated.  Otherwise every face is summed as the reference does.
+__device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, int NV, int NF,
+                                            f3 pt, f3 cj,
+                            float emax, unsigned *nearm, int lane) {
+  const float four_pi = 4.0f * (float)M_PI;
+  const f3 du = pt - cj;
+  const float r = sqrtf(dot(du, du));
+  bool outside = false;
+  if (r > 0.0f) {
+    // support of the neighbour's vertices along u = (pt - cj)/|pt - cj|,
+    // and the vertices within the drop range of pt
+    const f3 u = du / r;
+    const float dn = 1.3f * emax;
+    const float dn2 = dn * dn;
+    float h = -INFINITY;
+    for (int base = 0; base < NV; base += 32) {
+      const int k = base + lane;
+      bool nr = false;
+      if (k < NV) {
+        const f3 q = nbv(s, k);
+        h = fmaxf(h, dot(q - cj, u));
+        const f3 d = q - pt;
+        nr = dot(d, d) <= dn2;
+      }
+      const unsigned b = __ballot_sync(kFull, nr);
+      if (lane == 0) nearm[base >> 5] = b;
+    }
+    h = warp_max(h);
+    // rounding of the dot products is far below this margin
+    outside = r > h + 1e-5f * (1.0f + r + fabsf(h));
+    __syncwarp();
+  }
+  if (outside) {
+    float sum = 0.0f;
+    for (int wd = 0; wd < (NV + 31) / 32; ++wd) {
+      unsigned bits = nearm[wd];
+      while (bits) {
+        const int a0 = wd * 32 + __ffs(bits) - 1;
+        bits &= bits - 1u;
+        const int e0 = m.inc_off[a0], e1 = m.inc_off[a0 + 1];
+        for (int e = e0 + lane; e < e1; e += 32) {
+          const int f = m.inc_face[e];
+          const int i0 = s.faces[3 * f], i1 = s.faces[3 * f + 1], i2 = s.faces[3 * f + 2];
+          // each face once: at its lowest-numbered near corner
+          int low = NV;
+          if (near_bit(nearm, i0)) low = min(low, i0);
+          if (near_bit(nearm, i1)) low = min(low, i1);
+          if (near_bit(nearm, i2)) low = min(low, i2);
+          if (low != a0) continue;
+          float num, denom;
+          face_term(s, i0, i1, i2, pt, num, denom);
+          if (denom < 1e-8f) sum += 2.0f * atan2f(num, denom);
+        }
+      }
+    }
+    __syncwarp();
+    return -warp_sum(sum) / four_pi;
+  }
+  float part = 0.0f;
+  for (int f = lane; f < NF; f += 32) {
+    float num, denom;
+    face_term(s, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num, denom);
+    if (denom < 1e-8f) continue;
+    part += 2.0f * atan2f(num, denom);
+  }
+  return warp_sum(part) / four_pi;
+}
 
 __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
   extern __shared__ __align__(16) char smem3d[];
@@ -326,7 +426,6 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
     const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
     const int *list = a.nbr + (size_t)c * kMaxNB3D;
     const float L = T.L;
-    const float four_pi = 4.0f * (float)M_PI;
     for (int q = 0; q < count; ++q) {
       const int j = scan_all ? T.cell_begin + q : list[q];
       if (j == c) continue;
@@ -361,28 +460,11 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
           s.qz[k] = a.zin[bj + k] + shift.z;
         }
         __syncthreads();
-        float *ux = s.ux + w * NV, *uy = s.uy + w * NV, *uz = s.uz + w * NV;
+        unsigned *nearm = s.near + w * kNearWords;
         for (int i = w; i < ncand; i += kWarps) {
           const int v = s.cand[i];
           const f3 pt = vtx(s, v);
-          for (int k = lane; k < NV; k += 32) {
-            const f3 u = normalize(mk(s.qx[k], s.qy[k], s.qz[k]) - pt);
-            ux[k] = u.x;
-            uy[k] = u.y;
-            uz[k] = u.z;
-          }
-          __syncwarp();
-          float part = 0.0f;
-          for (int f = lane; f < NF; f += 32) {
-            const int i0 = s.faces[3 * f], i1 = s.faces[3 * f + 1], i2 = s.faces[3 * f + 2];
-            const f3 u = mk(ux[i0], uy[i0], uz[i0]), vv = mk(ux[i1], uy[i1], uz[i1]),
-                     ww = mk(ux[i2], uy[i2], uz[i2]);
-            const float denom = 1.0f + dot(u, vv) + dot(vv, ww) + dot(ww, u);
-            if (denom < 1e-8f) continue;
-            const float num = dot(u, cross(vv, ww));
-            part += 2.0f * atan2f(num, denom);
-          }
-          const float wn = warp_sum(part) / four_pi;
+          const float wn = winding_at(s, a.mesh, NV, NF, pt, cj, gj.emax, nearm, lane);
           if (lane == 0 && !(fabsf(wn) < 1e-6f)) {
             const f3 dir = normalize(C - pt);
             const float sc = fabsf(wn) * 0.5f * T.Kre;
@@ -604,7 +686,8 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
 } // namespace
 
 size_t step3d_smem_bytes(int nv, int nf, bool bend) {
-  size_t floats = (size_t)9 * nv + (size_t)3 * kWarps * nv + 64 + (bend ? (size_t)7 * nf : 0) + 4;
+  size_t floats = (size_t)9 * nv + 64 + (size_t)kWarps * kNearWords +
+                  (bend ? (size_t)7 * nf : 0) + 4;
   size_t halves = (size_t)3 * nf + nv;
   return floats * 4 + halves * 2 + (size_t)nv + 16;
 }
