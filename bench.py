@@ -240,6 +240,22 @@ def launches_per_call(batch, sim_steps, period):
     return blocks * (1 + 3 * passes + 1) + sim_steps
 
 
+def reduce_over_ranks(secs, units, world, device):
+    """Whole-job timing of independent shards: the slowest rank's time and
+    the units of all ranks (one all-reduce each, outside the timed region;
+    the shards exchange nothing while stepping)."""
+    if world <= 1:
+        return secs, units
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.barrier()
+    return float(t.item()), float(u.item())
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -287,13 +303,9 @@ def run_ours(args, rank, world, local_rank):
     secs = timed(b, args.steps, lambda: b.step(SIM_STEPS, DT))
     clock_info = clocks.stop()
     torch.cuda.synchronize()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([secs], device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = float(t.item())
-        dist.barrier()
-    value = V * SIM_STEPS * args.steps * world / secs
+    secs, units = reduce_over_ranks(secs, float(V) * SIM_STEPS * args.steps, world,
+                                    f"cuda:{local_rank}")
+    value = units / secs
     ms_per_step = secs / args.steps * 1e3
 
     if rank != 0:
@@ -354,6 +366,7 @@ def run_ours(args, rank, world, local_rank):
              "tuning": ptuned}
 
     p3 = plain3d(ctx, lambda n, fn: timed(None, n, fn), max(3, args.steps))
+    disp = disperse_leg(ctx, tissues)
 
     served = None
     if args.serve_requests > 0:
@@ -376,6 +389,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "e2e": e2e, "plain": plain,
         "batched_over_plain": round(value / world / plain["value"], 2),
         "plain3d": p3,
+        "disperse": disp,
         "served": served,
         "clocks": clock_info,
     }
@@ -440,6 +454,49 @@ def plain3d(ctx, timed, iters, steps=16):
             "workload": "1 monolayer, 256 cells x 642 vertices (icosphere subdivision 3), "
                         "jittered hexagonal lattice on z=0, kv=1 ka=0.5 ks=0.1 kb=0.05, "
                         "adhesion 0.1, dt=0.002"}
+
+
+def disperse_leg(ctx, tissues):
+    """Setup cost: the reference's dispersion of cell centres (bit-exact on
+    the device, dpm_disperse) for every tissue of the batched workload in one
+    launch, and for the 1,024-cell plain tissue; the host loop on a few
+    64-cell tissues for comparison."""
+    from opencl_dpm_gb300 import clDPM
+    from opencl_dpm_gb300.abi import disperse
+
+    def centres(ts, seed0):
+        X, Y = [], []
+        for k, t in enumerate(ts):
+            x, y = clDPM.drand48_centres(seed0 + k, len(t["nv"]), float(t["L"]))
+            X.append(np.asarray(x, np.float32))
+            Y.append(np.asarray(y, np.float32))
+        return np.concatenate(X), np.concatenate(Y)
+
+    def run(ts, seed0):
+        X, Y = centres(ts, seed0)
+        t0 = time.perf_counter()
+        _, _, it = disperse(ctx, [len(t["nv"]) for t in ts],
+                            np.concatenate([t["r0"] for t in ts]), [t["L"] for t in ts], X, Y)
+        return time.perf_counter() - t0, it
+
+    batch_s, batch_it = run(tissues, 1)
+    plain = workload_plain()
+    plain_s, plain_it = run(plain, 7)
+    # host loop on the four tissues nearest 64 cells, and the device on the same
+    near = sorted(range(len(tissues)), key=lambda k: abs(len(tissues[k]["nv"]) - 64))[:4]
+    sample = [tissues[k] for k in near]
+    t0 = time.perf_counter()
+    host_it = [clDPM.relax_centres(list(map(float, t["r0"])), float(t["L"]), 100 + k, False)[2]
+               for k, t in enumerate(sample)]
+    host_s = time.perf_counter() - t0
+    dev_s, dev_it = run(sample, 100)
+    return {"batched_tissues": len(tissues), "batched_s": round(batch_s, 3),
+            "batched_max_iterations": int(batch_it.max()),
+            "plain_1024_s": round(plain_s, 3), "plain_1024_iterations": int(plain_it[0]),
+            "host_sample": {"tissues": len(sample), "cells": [len(t["nv"]) for t in sample],
+                            "host_s": round(host_s, 3), "device_s": round(dev_s, 3),
+                            "iterations_equal": [int(a) for a in dev_it] == host_it},
+            "note": "bit-exact with the reference's host loop; one thread block per tissue"}
 
 
 def make_server(ctx):

@@ -222,6 +222,23 @@ int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel);
 int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts);
 
 /* ---------------------------------------------------------------------- */
+/* Dispersion of cell centres                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Relaxes the centres of nsystems independent systems of soft discs, as the
+ * loop of Tissue2D::Disperse (src/Tissue2D.cpp:53-104) and
+ * Tissue3D::Disperse2D (src/Tissue3D.cpp:40-106), bit for bit: overlap
+ * force (1 - d/(ri+rj))/(ri+rj) over periodic offsets, step 0.01, until the
+ * energy changes by at most 1e-6 or after 1e5 iterations.  ncells[s] cells
+ * (<= 4096) per system, concatenated in radius, X, Y; L[s] the box side.
+ * X, Y hold the starting centres (the reference draws them with drand48)
+ * and receive the relaxed ones; iterations[s] (may be NULL) the iteration
+ * count, above 1e5 when the cap was hit.  One thread block per system. */
+int dpm_disperse(dpm_ctx *ctx, int nsystems, const int *ncells,
+                 const float *radius, const float *L, float *X, float *Y,
+                 int *iterations);
+
+/* ---------------------------------------------------------------------- */
 /* Serving: continuous batching of independent simulation requests.       */
 /* The reference runs one Tissue per process, looping CLEulerUpdate        */
 /* (src/Tissue2D.cpp:116-241, src/Tissue3D.cpp:118-522); a server keeps     */

@@ -65,6 +65,8 @@ SIGNATURES = {
     "dpm2d_step_noalloc": (ctypes.c_int, [ctypes.c_int, _c_uint_p] + [_c_float_p] * 6 +
                            [ctypes.c_float] * 3 + [ctypes.c_int, _vp, _vp, ctypes.c_int,
                                                    ctypes.c_float, _vp]),
+    "dpm_disperse": (ctypes.c_int, [_vp, ctypes.c_int, _c_int_p, _c_float_p, _c_float_p,
+                                    _c_float_p, _c_float_p, _c_int_p]),
     "dpm_serve_create": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(_vp)]),
     "dpm_serve_destroy": (ctypes.c_int, [_vp]),
     "dpm_serve_add_pool2d": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -354,6 +356,20 @@ class Batch3D:
             self.close()
         except Exception:
             pass
+
+
+def disperse(ctx: Context, ncells, radius, L, X, Y):
+    """dpm_disperse: relaxed centres (X, Y) and iteration counts of
+    len(ncells) systems, one thread block each."""
+    nc = np.ascontiguousarray(ncells, dtype=np.int32)
+    r = _f32(radius)
+    Ls = _f32(np.broadcast_to(L, (len(nc),)))
+    x = _f32(X).copy()
+    y = _f32(Y).copy()
+    it = np.zeros(len(nc), np.int32)
+    check(ctx.lib.dpm_disperse(ctx.h, len(nc), nc.ctypes.data_as(_c_int_p), fptr(r), fptr(Ls),
+                               fptr(x), fptr(y), it.ctypes.data_as(_c_int_p)))
+    return x, y, it
 
 
 class Server:

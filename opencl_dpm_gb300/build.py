@@ -87,6 +87,7 @@ def build_library(verbose: bool = False, jobs: int = 8) -> str:
             continue
         if src.endswith(".cu"):
             cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-Xcompiler", "-ffp-contract=off",
                    "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
         else:
             cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-I", os.path.join(ROOT, "include"),
@@ -119,7 +120,10 @@ def build_module(verbose: bool = False) -> str:
     incs = []
     for i in pybind_includes():
         incs += ["-I", i]
-    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden", *incs,
+    # no FMA contraction: host geometry and dispersion reproduce the
+    # reference's separately rounded float operations on x86 and Arm alike
+    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden",
+          "-ffp-contract=off", *incs,
           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CSRC, "host"), *srcs,
           "-o", tmp, "-L", PKG, "-ldpm_gb300", "-Wl,-rpath,$ORIGIN"], verbose)
     os.replace(tmp, out)

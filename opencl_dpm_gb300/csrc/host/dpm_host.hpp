@@ -23,6 +23,13 @@ namespace DPM {
 // Disperse/Disperse2D like the reference's unseeded drand48() calls.
 void seed48(long seed);
 double rand48();
+// The starting centres of a dispersion after seed48(seed): X[i], Y[i] drawn
+// in turn as (float)(drand48() * L).
+void draw_centres(long seed, int n, float L, std::vector<float> &X, std::vector<float> &Y);
+// seed48(seed), then the dispersion loop (host or device); returns the
+// iteration count.
+int relax_centres(const std::vector<float> &radius, float L, long seed, bool device,
+                  std::vector<float> &X, std::vector<float> &Y);
 
 // Process-wide library context on the device named by $DPM_DEVICE (default 0).
 dpm_ctx *default_context();
@@ -96,7 +103,8 @@ public:
   ~Tissue2D();
   Tissue2D(const Tissue2D &o);
   Tissue2D &operator=(const Tissue2D &o);
-  void Disperse();
+  // device: relax on the GPU (dpm_disperse, same bits); false: on the host
+  void Disperse(bool device = true);
   void CLEulerUpdate(int nsteps, float dt);
   // extensions
   void SetPackingFraction(float phi);
@@ -123,7 +131,7 @@ public:
   Tissue3D(const Tissue3D &o);
   Tissue3D &operator=(const Tissue3D &o);
   void CLEulerUpdate(int nsteps, float dt);
-  void Disperse2D();
+  void Disperse2D(bool device = true);
 
 private:
   dpm3d_batch *batch_ = nullptr;

@@ -41,7 +41,8 @@ PYBIND11_MODULE(clDPM, m) {
       .def_readwrite("Kre", &DPM::Tissue2D::Kre)
       .def_readwrite("Kat", &DPM::Tissue2D::Kat)
       .def("CLEulerUpdate", &DPM::Tissue2D::CLEulerUpdate, py::arg("nsteps"), py::arg("dt"))
-      .def("Disperse", &DPM::Tissue2D::Disperse)
+      .def("Disperse", &DPM::Tissue2D::Disperse, py::arg("device") = true,
+           "device (extension): relax on the GPU, bit for bit the host loop; False: host")
       // extensions
       .def("SetPackingFraction", &DPM::Tissue2D::SetPackingFraction,
            "extension: rescale the box and cell centroids to true packing fraction phi")
@@ -88,8 +89,27 @@ PYBIND11_MODULE(clDPM, m) {
       .def_readonly("L", &DPM::Tissue3D::L)
       .def_readonly("PBC", &DPM::Tissue3D::PBC)
       .def("CLEulerUpdate", &DPM::Tissue3D::CLEulerUpdate, py::arg("nsteps"), py::arg("dt"))
-      .def("Disperse2D", &DPM::Tissue3D::Disperse2D);
+      .def("Disperse2D", &DPM::Tissue3D::Disperse2D, py::arg("device") = true,
+           "device (extension): relax on the GPU, bit for bit the host loop; False: host");
 
+  m.def(
+      "drand48_centres",
+      [](long seed, int n, float L) {
+        std::vector<float> X, Y;
+        DPM::draw_centres(seed, n, L, X, Y);
+        return py::make_tuple(X, Y);
+      },
+      py::arg("seed"), py::arg("n"), py::arg("L"),
+      "extension: the starting centres a dispersion draws after srand48(seed)");
+  m.def(
+      "relax_centres",
+      [](std::vector<float> radius, float L, long seed, bool device) {
+        std::vector<float> X, Y;
+        const int count = DPM::relax_centres(radius, L, seed, device, X, Y);
+        return py::make_tuple(X, Y, count);
+      },
+      py::arg("radius"), py::arg("L"), py::arg("seed"), py::arg("device") = true,
+      "extension: srand48(seed), then the dispersion loop; (X, Y, iterations)");
   m.def("srand48", &DPM::seed48,
         "extension: seed the dispersion generator (the reference uses unseeded drand48)");
   m.def("version", []() { return std::string(dpm_version()); });

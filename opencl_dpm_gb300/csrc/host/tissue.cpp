@@ -56,8 +56,8 @@ namespace {
 // Soft-disk relaxation of centres (src/Tissue2D.cpp:42-105,
 // src/Tissue3D.cpp:40-106): drand48 centres in [0, L), overlap force
 // (1 - d/(ri+rj))/(ri+rj), step 0.01, until |dU| <= 1e-6 or 1e5 iterations.
-void relax(const std::vector<float> &radius, float L, std::vector<float> &X,
-           std::vector<float> &Y, bool warn) {
+int relax(const std::vector<float> &radius, float L, std::vector<float> &X,
+          std::vector<float> &Y, bool warn, bool device) {
   const int n = (int)radius.size();
   X.resize(n);
   Y.resize(n);
@@ -65,6 +65,15 @@ void relax(const std::vector<float> &radius, float L, std::vector<float> &X,
   for (int i = 0; i < n; i++) {
     X[i] = (float)(rand48() * L);
     Y[i] = (float)(rand48() * L);
+  }
+  if (device) {
+    // the same loop on the GPU, bit for bit
+    int count = 0;
+    check(dpm_disperse(default_context(), 1, &n, radius.data(), &L, X.data(), Y.data(), &count),
+          "dpm_disperse");
+    if (warn && count > 100000)
+      std::cerr << "Warning: Max timesteps for dispersion reached" << std::endl;
+    return count;
   }
   float oldU = 100, dU = 100;
   int count = 0;
@@ -109,9 +118,26 @@ void relax(const std::vector<float> &radius, float L, std::vector<float> &X,
       break;
     }
   }
+  return count;
 }
 
 } // namespace
+
+void draw_centres(long seed, int n, float L, std::vector<float> &X, std::vector<float> &Y) {
+  seed48(seed);
+  X.resize(n);
+  Y.resize(n);
+  for (int i = 0; i < n; i++) {
+    X[i] = (float)(rand48() * L);
+    Y[i] = (float)(rand48() * L);
+  }
+}
+
+int relax_centres(const std::vector<float> &radius, float L, long seed, bool device,
+                  std::vector<float> &X, std::vector<float> &Y) {
+  seed48(seed);
+  return relax(radius, L, X, Y, false, device);
+}
 
 // ---------------------------------------------------------------------------
 // Tissue2D
@@ -156,10 +182,10 @@ void Tissue2D::release() {
 }
 
 // src/Tissue2D.cpp:42-114: relax centres, then regular polygons around them.
-void Tissue2D::Disperse() {
+void Tissue2D::Disperse(bool device) {
   std::vector<float> r(NCELLS), X, Y;
   for (int i = 0; i < NCELLS; i++) r[i] = cells[i].r0;
-  relax(r, L, X, Y, false);
+  relax(r, L, X, Y, false, device);
   for (int i = 0; i < NCELLS; i++)
     for (unsigned j = 0; j < cells[i].NV; j++) {
       const double ang = 2.0 * M_PI * (j + 1) / cells[i].NV;
@@ -304,10 +330,10 @@ void Tissue3D::release() {
 }
 
 // src/Tissue3D.cpp:40-116 (cells move to -(X, Y), as in the reference)
-void Tissue3D::Disperse2D() {
+void Tissue3D::Disperse2D(bool device) {
   std::vector<float> r(NCELLS), X, Y;
   for (int i = 0; i < NCELLS; i++) r[i] = Cells[i].r0 * 2;
-  relax(r, L, X, Y, true);
+  relax(r, L, X, Y, true, device);
   for (int i = 0; i < NCELLS; i++) {
     const std::array<float, 3> com = Cells[i].GetCOM();
     for (auto &v : Cells[i].Verts) {

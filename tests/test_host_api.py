@@ -87,13 +87,13 @@ def test_tissue2d_box(clDPM):
     assert np.float32(T.L) == g["L"] and T.NCELLS == 16 and T.PBC
 
 
-def test_disperse(clDPM):
+def check_disperse(clDPM, device):
     g = load("disperse_2d")
     cells = [clDPM.Cell2D(0.0, 0.0, 1.0, int(nv), float(r)) for nv, r in zip(g["nv"], g["r0"])]
     T = clDPM.Tissue2D(cells, float(g["phi0"]))
     assert np.float32(T.L) == g["L"]
     clDPM.srand48(int(g["seed"]))
-    T.Disperse()
+    T.Disperse(device=device)
     xy = np.concatenate([np.array(c.Verts, np.float32) for c in T.Cells])
     assert np.array_equal(xy, g["xy"])
     g3 = load("disperse_3d")
@@ -101,9 +101,50 @@ def test_disperse(clDPM):
     T3 = clDPM.Tissue3D(c3, float(g3["phi0"]))
     assert np.float32(T3.L) == g3["L"]
     clDPM.srand48(int(g3["seed"]))
-    T3.Disperse2D()
+    T3.Disperse2D(device=device)
     x3 = np.concatenate([np.array(c.Verts, np.float32) for c in T3.Cells])
     assert np.array_equal(x3, g3["xyz"])
+
+
+def test_disperse_host(clDPM):
+    """The host loop reproduces the reference build's dispersion bit for bit."""
+    check_disperse(clDPM, device=False)
+
+
+@pytest.mark.gpu
+def test_disperse_device(clDPM):
+    """The device relaxation reproduces the same bits."""
+    check_disperse(clDPM, device=True)
+
+
+@pytest.mark.gpu
+def test_disperse_device_batched(clDPM):
+    """Many systems in one launch, each equal to the host loop; sizes span
+    the list overflow (dense) and the skin rebuilds (sparse)."""
+    from opencl_dpm_gb300.abi import Context, disperse
+    rng = np.random.default_rng(9)
+    systems = []
+    for n in (1, 2, 17, 64, 200):
+        r = rng.choice([1.0, 1.4], n).astype(np.float32)
+        # box for true packing fraction phi: L = sqrt(sum pi r^2 / phi)
+        L = np.float32(np.sqrt(np.sum(np.pi * r.astype(np.float64) ** 2) / rng.uniform(0.3, 0.9)))
+        systems.append((r, L, 1000 + n))
+    X0, Y0 = [], []
+    for r, L, seed in systems:
+        x, y = clDPM.drand48_centres(seed, len(r), float(L))
+        X0.append(np.asarray(x, np.float32))
+        Y0.append(np.asarray(y, np.float32))
+    ctx = Context(0)
+    X, Y, it = disperse(ctx, [len(s[0]) for s in systems], np.concatenate([s[0] for s in systems]),
+                        [s[1] for s in systems], np.concatenate(X0), np.concatenate(Y0))
+    off = 0
+    for (r, L, seed), k in zip(systems, it):
+        n = len(r)
+        hx, hy, hk = clDPM.relax_centres(list(map(float, r)), float(L), seed, False)
+        assert np.array_equal(X[off:off + n], np.asarray(hx, np.float32))
+        assert np.array_equal(Y[off:off + n], np.asarray(hy, np.float32))
+        assert k == hk
+        off += n
 
 
 def test_tissue3d_validation(clDPM):
