@@ -124,6 +124,15 @@ int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant);
 int dpm2d_last_contained(dpm2d_batch *b, unsigned char *flags);
 int dpm2d_cell_areas(dpm2d_batch *b, float *area);
 int dpm2d_stats(dpm2d_batch *b, long *rebuilds, long *fallback_steps);
+/* Ensemble diagnostics of the current state, computed on the device in
+ * double (any output may be NULL).  Per cell: |area|, perimeter and the
+ * energy Ka/2 (A/a0-1)^2 + Kl/2 sum (l/l0-1)^2 + Kb/2 sum |s_i|^2 (project-
+ * defined; the reference has none, and its area force is not this energy's
+ * gradient).  Per tissue: packing fraction sum(A)/L^2 and the mean shape
+ * index P/sqrt(4 pi A). */
+int dpm2d_diagnostics(dpm2d_batch *b, double *area, double *perimeter,
+                      double *energy, double *packing_fraction,
+                      double *shape_index);
 
 /* Cell-list snapshot for host verification (see dpm2d_rebuild_now):
  * sorted bin keys and cell ids (uint32[ncells] each), per-cell neighbour
@@ -220,6 +229,13 @@ int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel);
 /* Per-vertex count of other cells whose winding number passed the
  * reference's threshold in the last step (uint8 per vertex). */
 int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts);
+/* Per-cell diagnostics of the current state, computed on the device in
+ * double (any output may be NULL): enclosed volume and surface area
+ * (Cell3D::GetVolume / GetSurfaceArea, src/cell.cpp:196-230, for every
+ * cell at once) and the energy Kv/2 (V/v0-1)^2 + Ka/2 sum_edges (l/l0-1)^2
+ * + Kb sum_edges (1 - n1.n2) (project-defined; the reference has none). */
+int dpm3d_diagnostics(dpm3d_batch *b, double *volume, double *surface_area,
+                      double *energy);
 
 /* ---------------------------------------------------------------------- */
 /* Dispersion of cell centres                                              */

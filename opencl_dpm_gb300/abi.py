@@ -65,6 +65,8 @@ SIGNATURES = {
     "dpm2d_step_noalloc": (ctypes.c_int, [ctypes.c_int, _c_uint_p] + [_c_float_p] * 6 +
                            [ctypes.c_float] * 3 + [ctypes.c_int, _vp, _vp, ctypes.c_int,
                                                    ctypes.c_float, _vp]),
+    "dpm2d_diagnostics": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_double)] * 5),
+    "dpm3d_diagnostics": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_double)] * 3),
     "dpm_disperse": (ctypes.c_int, [_vp, ctypes.c_int, _c_int_p, _c_float_p, _c_float_p,
                                     _c_float_p, _c_float_p, _c_int_p]),
     "dpm_serve_create": (ctypes.c_int, [_vp, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -206,6 +208,16 @@ class Batch2D:
     def set_kernel_variant(self, variant: int):
         check(self.lib.dpm2d_set_kernel_variant(self.h, variant))
 
+    def diagnostics(self) -> dict:
+        """Per cell area, perimeter, energy; per tissue packing fraction and
+        mean shape index (double, computed on the device)."""
+        d = ctypes.POINTER(ctypes.c_double)
+        a, p, e = (np.zeros(self.ncells) for _ in range(3))
+        phi, si = np.zeros(self.ntissues), np.zeros(self.ntissues)
+        check(self.lib.dpm2d_diagnostics(self.h, *[x.ctypes.data_as(d) for x in (a, p, e, phi, si)]))
+        return {"area": a, "perimeter": p, "energy": e, "packing_fraction": phi,
+                "shape_index": si}
+
     def upload(self, xy):
         xy = _f32(xy)
         assert xy.size == 2 * self.nverts
@@ -345,6 +357,13 @@ class Batch3D:
         f = np.empty(self.nverts, np.uint8)
         check(self.lib.dpm3d_last_winding(self.h, f.ctypes.data_as(_c_ubyte_p)))
         return f
+
+    def diagnostics(self) -> dict:
+        """Per cell volume, surface area and energy (double, on the device)."""
+        d = ctypes.POINTER(ctypes.c_double)
+        v, a, e = (np.zeros(self.ncells) for _ in range(3))
+        check(self.lib.dpm3d_diagnostics(self.h, *[x.ctypes.data_as(d) for x in (v, a, e)]))
+        return {"volume": v, "surface_area": a, "energy": e}
 
     def close(self):
         if self.h:

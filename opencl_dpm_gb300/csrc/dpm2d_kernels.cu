@@ -155,6 +155,50 @@ __global__ void __launch_bounds__(kGeomWarps * 32)
 }
 
 // ---------------------------------------------------------------------------
+// Diagnostics (double precision, one warp per cell)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// Per cell: |area| (shoelace), perimeter, sum over edges of (l/l0 - 1)^2 and
+// sum over vertices of |s_i|^2, s_i = (x_{i+1} - x_i) - (x_i - x_{i-1}).
+__global__ void __launch_bounds__(kGeomWarps * 32)
+    k2d_diag(const Cell2D *__restrict__ cells, const float2 *__restrict__ pos, double4 *out,
+             int ncells) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kGeomWarps + w;
+  if (c >= ncells) return;
+  const Cell2D cp = cells[c];
+  const int n = (int)cp.nv;
+  if (n == 0) {
+    if (lane == 0) out[c] = make_double4(0.0, 0.0, 0.0, 0.0);
+    return;
+  }
+  const float2 *p = pos + cp.voff;
+  double A = 0.0, P = 0.0, Ul = 0.0, Ub = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const int j = i + 1 == n ? 0 : i + 1, k = i == 0 ? n - 1 : i - 1;
+    const double xi = p[i].x, yi = p[i].y, xj = p[j].x, yj = p[j].y, xk = p[k].x, yk = p[k].y;
+    A += xi * yj - xj * yi;
+    const double l = sqrt((xj - xi) * (xj - xi) + (yj - yi) * (yj - yi));
+    P += l;
+    const double dl = l / (double)cp.l0 - 1.0;
+    Ul += dl * dl;
+    const double sx = (xj - xi) - (xi - xk), sy = (yj - yi) - (yi - yk);
+    Ub += sx * sx + sy * sy;
+  }
+  A = warp_sum_d(A);
+  P = warp_sum_d(P);
+  Ul = warp_sum_d(Ul);
+  Ub = warp_sum_d(Ub);
+  if (lane == 0) out[c] = make_double4(fabs(0.5 * A), P, Ul, Ub);
+}
+
+// ---------------------------------------------------------------------------
 // Cell list: per-tissue bins and keys
 // ---------------------------------------------------------------------------
 
@@ -801,6 +845,13 @@ cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom, 
   (void)maxnv;
   const int grid = (ncells + kGeomWarps - 1) / kGeomWarps;
   k2d_geom<<<grid, kGeomWarps * 32, 0, s>>>(cells, pos, geom, ncells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diag2d(const Cell2D *cells, const float2 *pos, double4 *out, int ncells,
+                          cudaStream_t s) {
+  const int grid = (ncells + kGeomWarps - 1) / kGeomWarps;
+  k2d_diag<<<grid, kGeomWarps * 32, 0, s>>>(cells, pos, out, ncells);
   return cudaGetLastError();
 }
 

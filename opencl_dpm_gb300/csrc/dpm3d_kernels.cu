@@ -531,6 +531,88 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------------------------------------------------------------------
+// Diagnostics (double precision, one block per cell)
+// ---------------------------------------------------------------------------
+
+__device__ double block_sum_d(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int i = 0; i < kWarps; ++i) r += red[i];
+  return r;
+}
+
+// Per cell: enclosed volume, surface area and the energy
+// Kv/2 (V/v0 - 1)^2 + Ka/2 sum_edges (l/l0 - 1)^2 + Kb sum_edges (1 - n1.n2)
+// (project-defined; the reference defines no energy), all in double.
+__global__ void __launch_bounds__(kThreads)
+    k3d_diag(const float *x, const float *y, const float *z, Mesh3D mesh, const Cell3D *cells,
+             double *out, int nv) {
+  __shared__ double red[kWarps];
+  const Cell3D P = cells[blockIdx.x];
+  double *o = out + 3 * (size_t)blockIdx.x;
+  if (!P.active) {
+    if (threadIdx.x == 0) o[0] = o[1] = o[2] = 0.0;
+    return;
+  }
+  const size_t base = (size_t)blockIdx.x * nv;
+  auto vd = [&](int i) {
+    return make_double3((double)x[base + i], (double)y[base + i], (double)z[base + i]);
+  };
+  auto normal = [&](int f, double3 &n) {
+    const double3 a = vd(mesh.faces[3 * f]), b = vd(mesh.faces[3 * f + 1]),
+                  d = vd(mesh.faces[3 * f + 2]);
+    const double ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z;
+    const double wx = d.x - a.x, wy = d.y - a.y, wz = d.z - a.z;
+    n = make_double3(uy * wz - uz * wy, uz * wx - ux * wz, ux * wy - uy * wx);
+    return sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+  };
+  double V = 0.0, A = 0.0, Ue = 0.0, Eb = 0.0;
+  for (int f = threadIdx.x; f < mesh.nf; f += kThreads) {
+    const int i0 = mesh.faces[3 * f], i1 = mesh.faces[3 * f + 1], i2 = mesh.faces[3 * f + 2];
+    const double3 a = vd(i0), b = vd(i1), d = vd(i2);
+    V += a.x * (b.y * d.z - b.z * d.y) + a.y * (b.z * d.x - b.x * d.z) +
+         a.z * (b.x * d.y - b.y * d.x);
+    double3 n;
+    const double ln = normal(f, n);
+    A += 0.5 * ln;
+    const double3 e[3] = {a, b, d};
+    for (int k = 0; k < 3; ++k) {
+      const double3 s = e[k], q = e[(k + 1) % 3];
+      const double l =
+          sqrt((q.x - s.x) * (q.x - s.x) + (q.y - s.y) * (q.y - s.y) + (q.z - s.z) * (q.z - s.z));
+      const double dl = l / (double)P.l0 - 1.0;
+      Ue += 0.5 * dl * dl;  // each edge is seen from both of its faces
+      if (P.Kb != 0.0f) {
+        const int g = mesh.adj[3 * f + k];
+        if (g > f) {  // each edge once; a degenerate face has normal 0
+          double3 m;
+          const double lm = normal(g, m);
+          const double cth =
+              ln > 0.0 && lm > 0.0 ? (n.x * m.x + n.y * m.y + n.z * m.z) / (ln * lm) : 0.0;
+          Eb += 1.0 - cth;
+        }
+      }
+    }
+  }
+  V = block_sum_d(V, red);
+  A = block_sum_d(A, red);
+  Ue = block_sum_d(Ue, red);
+  Eb = block_sum_d(Eb, red);
+  if (threadIdx.x == 0) {
+    V = fabs(V) / 6.0;
+    const double dv = V / (double)P.v0 - 1.0;
+    o[0] = V;
+    o[1] = A;
+    o[2] = 0.5 * (double)P.Kv * dv * dv + 0.5 * (double)P.Ka * Ue + (double)P.Kb * Eb;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Cell list (3D): periodic bins of the centres, sorted keys, neighbour lists
 // ---------------------------------------------------------------------------
 
@@ -700,6 +782,12 @@ cudaError_t prepare_step3d(int nv, int nf, bool bend) {
 cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {
   const size_t bytes = step3d_smem_bytes(a.mesh.nv, a.mesh.nf, a.bend != 0);
   k3d_step<<<a.ncells, kThreads, bytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diag3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
+                          const Cell3D *cells, double *out, int ncells, cudaStream_t s) {
+  k3d_diag<<<ncells, kThreads, 0, s>>>(x, y, z, mesh, cells, out, mesh.nv);
   return cudaGetLastError();
 }
 

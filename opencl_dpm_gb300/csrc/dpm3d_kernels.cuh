@@ -49,6 +49,9 @@ struct Rebuild3DArgs {
 
 cudaError_t launch_geom3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
                           const Cell3D *cells, Geom3D *geom, int ncells, cudaStream_t s);
+// Per cell, in double: (volume, surface area, energy) into out[3*c .. 3*c+2].
+cudaError_t launch_diag3d(const float *x, const float *y, const float *z, const Mesh3D &mesh,
+                          const Cell3D *cells, double *out, int ncells, cudaStream_t s);
 cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 size_t step3d_smem_bytes(int nv, int nf, bool bend);

@@ -12,11 +12,16 @@
 // -f(k, j) over its contacts j < k, then over all its contacts, then over its
 // contacts j > k (rows i < k add to F[k] before row k, rows i > k after).
 // Each thread folds that sequence for its cells, every operation rounded as
-// in the reference (float, with the reference's double sub-expressions);
-// one thread then adds the U terms in row order.  Contacts come from
-// per-cell lists of the cells within the contact distance plus a skin,
-// rebuilt when some centre has moved by half the skin, and kept in
+// in the reference; one thread then adds the U terms in row order.
+// Contacts come from per-cell lists of the cells within the contact distance
+// plus a skin, rebuilt when some centre has moved by half the skin, kept in
 // ascending order; the contact test itself is the reference's.
+//
+// Where the reference rounds a double expression of float operands to float
+// and the double operation is exact (or is a correctly rounded sqrt, which
+// rounds to float without double-rounding error since 53 >= 2*24 + 2), the
+// same bits come from the float operation; only the force magnitude
+// (1 - q)/(ri + rj) and the position update x + 0.01 F stay in double.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,6 +38,8 @@ constexpr int kDispThreads = 256;
 constexpr int kDispMaxNb = 48;       // list capacity per cell (more: scan all)
 constexpr int kDispMaxCells = 4096;  // per system (shared-memory staging)
 constexpr int kDispMaxIter = 100000; // the reference's cap (count > 1e5)
+constexpr int kDispTerms = 6;        // U terms per row kept in shared memory
+constexpr int kDispContacts = 24;    // contacts per cell folded from registers
 
 struct DisperseArgs {
   const int *begin;    // [nsys + 1] first cell of each system
@@ -42,47 +49,51 @@ struct DisperseArgs {
   int *count;          // [nsys] iterations run
   int *nb;             // [ncells * kDispMaxNb] contact candidates, ascending
   int *nn;             // [ncells] candidate count, -1: scan every cell
-  float *inner;        // [ncells * kDispMaxNb] U terms of each row's contacts
+  float *inner;        // [ncells * kDispMaxNb] U terms of rows with many contacts
 };
+
+// x - L round(x / L), rounded to float as the reference's
+// (float)((double)x - (double)L * round((double)(x / L))).
+__device__ __forceinline__ float wrap_ref(float x, float L) {
+  const float r = roundf(__fdiv_rn(x, L));
+  if (r == 0.0f) return x;
+  if (fabsf(r) == 1.0f) return __fsub_rn(x, r == 1.0f ? L : -L);  // exact in double
+  return __double2float_rn(__dsub_rn((double)x, __dmul_rn((double)L, (double)r)));
+}
 
 // The reference's wrapped offset from (xi, yi) to (xj, yj), distance, and
 // contact test dist <= ri + rj.
 __device__ __forceinline__ bool contact(float xi, float yi, float ri, float xj, float yj,
                                         float rj, float L, float &dx, float &dy, float &dist) {
-  dx = __fsub_rn(xj, xi);
-  dx = __double2float_rn(
-      __dsub_rn((double)dx, __dmul_rn((double)L, round((double)__fdiv_rn(dx, L)))));
-  dy = __fsub_rn(yj, yi);
-  dy = __double2float_rn(
-      __dsub_rn((double)dy, __dmul_rn((double)L, round((double)__fdiv_rn(dy, L)))));
-  dist = __double2float_rn(__dsqrt_rn((double)__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy))));
+  dx = wrap_ref(__fsub_rn(xj, xi), L);
+  dy = wrap_ref(__fsub_rn(yj, yi), L);
+  dist = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
   return dist <= __fadd_rn(ri, rj);
 }
 
-// Pair force (fx, fy) of the reference for a pair in contact.
-__device__ __forceinline__ void pair_force(float dx, float dy, float dist, float ri, float rj,
-                                           float &fx, float &fy) {
+// Pair force (fx, fy) and energy term 1 - q (1 - q), q = dist / (ri + rj),
+// of the reference for a pair in contact.
+__device__ __forceinline__ void pair_terms(float dx, float dy, float dist, float ri, float rj,
+                                           float &fx, float &fy, float &u) {
   const float ux = __fdiv_rn(dx, dist), uy = __fdiv_rn(dy, dist);
   const float s = __fadd_rn(ri, rj);
   const float q = __fdiv_rn(dist, s);
   const float ftmp = __double2float_rn(__ddiv_rn(__dsub_rn(1.0, (double)q), (double)s));
   fx = __fmul_rn(ftmp, ux);
   fy = __fmul_rn(ftmp, uy);
-}
-
-// The reference's energy term 1 - q (1 - q), q = dist / (ri + rj), in float.
-__device__ __forceinline__ float u_term(float dist, float ri, float rj) {
-  const float q = __fdiv_rn(dist, __fadd_rn(ri, rj));
-  return __fsub_rn(1.0f, __fmul_rn(q, __fsub_rn(1.0f, q)));
+  u = __fsub_rn(1.0f, __fmul_rn(q, __fsub_rn(1.0f, q)));
 }
 
 __global__ void __launch_bounds__(kDispThreads) k_disperse(DisperseArgs a) {
   extern __shared__ float sm[];
   __shared__ int s_rebuild, s_stop;
+  __shared__ float s_red[kDispThreads / 32];
   const int sys = blockIdx.x;
   const int c0 = a.begin[sys], n = a.begin[sys + 1] - c0;
   const float L = a.L[sys];
   float *X = sm, *Y = X + n, *X0 = Y + n, *Y0 = X0 + n, *R = Y0 + n;
+  float *T = R + n;                              // [n * kDispTerms] U terms
+  int *tc = reinterpret_cast<int *>(T + (size_t)n * kDispTerms);  // [n] U term counts
   const int tid = threadIdx.x;
   float rmin = INFINITY;
   for (int k = tid; k < n; k += kDispThreads) {
@@ -91,8 +102,7 @@ __global__ void __launch_bounds__(kDispThreads) k_disperse(DisperseArgs a) {
     R[k] = a.radius[c0 + k];
     rmin = fminf(rmin, R[k]);
   }
-  // skin of the contact lists: a fraction of the smallest radius
-  __shared__ float s_red[kDispThreads / 32];
+  // skin of the contact lists: half the smallest radius
   rmin = warp_min(rmin);
   if ((tid & 31) == 0) s_red[tid >> 5] = rmin;
   if (tid == 0) {
@@ -136,54 +146,98 @@ __global__ void __launch_bounds__(kDispThreads) k_disperse(DisperseArgs a) {
     // forces of this iteration, folded in the reference's order
     float fxk[(kDispMaxCells + kDispThreads - 1) / kDispThreads];
     float fyk[(kDispMaxCells + kDispThreads - 1) / kDispThreads];
+    bool rescan = false;  // a U row must be rescanned from the positions
 #pragma unroll 1
     for (int t = 0, k = tid; k < n; ++t, k += kDispThreads) {
       const float xk = X[k], yk = Y[k], rk = R[k];
       const int m = nn[k];
       const int *lst = nb + (size_t)k * kDispMaxNb;
       const int cnt = m < 0 ? n : m;
+      // contacts of row k in ascending order: pair force and U term
+      float cfx[kDispContacts], cfy[kDispContacts];
+      int nc = 0, nlt = 0;
+      bool many = false;
       float Fx = 0.0f, Fy = 0.0f;
-      // segment 1: contacts j < k; segment 2: all contacts (storing the U
-      // terms of row k); segment 3: contacts j > k
-      for (int seg = 0; seg < 3; ++seg) {
-        int u = 0;
-        for (int p = 0; p < cnt; ++p) {
-          const int j = m < 0 ? p : lst[p];
-          if (j == k) continue;
-          if (seg == 0 && j > k) break;
-          if (seg == 2 && j < k) continue;
-          float dx, dy, dist;
-          if (!contact(xk, yk, rk, X[j], Y[j], R[j], L, dx, dy, dist)) continue;
-          float fx, fy;
-          pair_force(dx, dy, dist, rk, R[j], fx, fy);
-          Fx = __fsub_rn(Fx, fx);
-          Fy = __fsub_rn(Fy, fy);
-          if (seg == 1 && m >= 0) inner[(size_t)k * kDispMaxNb + u++] = u_term(dist, rk, R[j]);
+      for (int p = 0; p < cnt; ++p) {
+        const int j = m < 0 ? p : lst[p];
+        if (j == k) continue;
+        float dx, dy, dist;
+        if (!contact(xk, yk, rk, X[j], Y[j], R[j], L, dx, dy, dist)) continue;
+        float fx, fy, u;
+        pair_terms(dx, dy, dist, rk, R[j], fx, fy, u);
+        if (nc < kDispTerms) T[(size_t)k * kDispTerms + nc] = u;
+        else if (m >= 0) inner[(size_t)k * kDispMaxNb + nc] = u;
+        if (nc < kDispContacts) {
+          cfx[nc] = fx;
+          cfy[nc] = fy;
+        } else {
+          many = true;
         }
-        if (seg == 1 && m >= 0) nn[k] = m | (u << 16);
+        nlt += j < k ? 1 : 0;
+        ++nc;
+      }
+      tc[k] = m < 0 && nc > kDispTerms ? -1 : nc;
+      rescan |= tc[k] < 0;
+      if (!many) {
+        // segment 1: j < k; segment 2: all; segment 3: j > k
+#pragma unroll 1
+        for (int p = 0; p < nlt; ++p) {
+          Fx = __fsub_rn(Fx, cfx[p]);
+          Fy = __fsub_rn(Fy, cfy[p]);
+        }
+#pragma unroll 1
+        for (int p = 0; p < nc; ++p) {
+          Fx = __fsub_rn(Fx, cfx[p]);
+          Fy = __fsub_rn(Fy, cfy[p]);
+        }
+#pragma unroll 1
+        for (int p = nlt; p < nc; ++p) {
+          Fx = __fsub_rn(Fx, cfx[p]);
+          Fy = __fsub_rn(Fy, cfy[p]);
+        }
+      } else {
+        // more contacts than registers hold: recompute per segment
+        for (int seg = 0; seg < 3; ++seg)
+          for (int p = 0; p < cnt; ++p) {
+            const int j = m < 0 ? p : lst[p];
+            if (j == k || (seg == 0 && j > k) || (seg == 2 && j < k)) continue;
+            float dx, dy, dist;
+            if (!contact(xk, yk, rk, X[j], Y[j], R[j], L, dx, dy, dist)) continue;
+            float fx, fy, u;
+            pair_terms(dx, dy, dist, rk, R[j], fx, fy, u);
+            Fx = __fsub_rn(Fx, fx);
+            Fy = __fsub_rn(Fy, fy);
+          }
       }
       fxk[t] = Fx;
       fyk[t] = Fy;
     }
-    __syncthreads();
+    // without rescans the U sum reads only stored terms, so the position
+    // update below may overlap it
+    const bool any_rescan = __syncthreads_or(rescan) != 0;
 
-    // U in row order (one thread), positions (every thread)
+    // U in row order (one thread): U = (float)((double)U + 0.5 * inner) is
+    // the float sum U + 0.5f * inner, the double sum being exact
     if (tid == 0) {
       float U = 0.0f;
       for (int k = 0; k < n; ++k) {
-        const int m = nn[k];
-        if (m >= 0) {
-          const int u = m >> 16;
-          for (int p = 0; p < u; ++p)
-            U = __double2float_rn(
-                __dadd_rn((double)U, __dmul_rn(0.5, (double)inner[(size_t)k * kDispMaxNb + p])));
+        const int u = tc[k];
+        if (u >= 0) {
+          const float *row = T + (size_t)k * kDispTerms;
+#pragma unroll
+          for (int p = 0; p < kDispTerms; ++p)
+            if (p < u) U = __fadd_rn(U, __fmul_rn(0.5f, row[p]));
+          for (int p = kDispTerms; p < u; ++p)
+            U = __fadd_rn(U, __fmul_rn(0.5f, inner[(size_t)k * kDispMaxNb + p]));
         } else {
+          // a row scanned in full with more terms than the buffers hold
           for (int j = 0; j < n; ++j) {
             if (j == k) continue;
             float dx, dy, dist;
             if (!contact(X[k], Y[k], R[k], X[j], Y[j], R[j], L, dx, dy, dist)) continue;
-            U = __double2float_rn(
-                __dadd_rn((double)U, __dmul_rn(0.5, (double)u_term(dist, R[k], R[j]))));
+            float fx, fy, uu;
+            pair_terms(dx, dy, dist, R[k], R[j], fx, fy, uu);
+            U = __fadd_rn(U, __fmul_rn(0.5f, uu));
           }
         }
       }
@@ -193,7 +247,7 @@ __global__ void __launch_bounds__(kDispThreads) k_disperse(DisperseArgs a) {
       ++count;
       s_stop = !((double)dU > 1e-6) || count > kDispMaxIter;
     }
-    __syncthreads();
+    if (any_rescan) __syncthreads();
     bool moved = false;
 #pragma unroll 1
     for (int t = 0, k = tid; k < n; ++t, k += kDispThreads) {
@@ -201,7 +255,6 @@ __global__ void __launch_bounds__(kDispThreads) k_disperse(DisperseArgs a) {
       Y[k] = __double2float_rn(__dadd_rn((double)Y[k], __dmul_rn(0.01, (double)fyk[t])));
       const float d = fabsf(X[k] - X0[k]) + fabsf(Y[k] - Y0[k]);
       moved |= !(d <= 0.5f * skin);
-      if (nn[k] >= 0) nn[k] &= 0xffff;
     }
     const bool any = __syncthreads_or(moved) != 0;
     if (tid == 0 && any) s_rebuild = 1;
@@ -256,9 +309,10 @@ extern "C" int dpm_disperse(dpm_ctx *ctx, int nsystems, const int *ncells, const
   DPM_CUDA_TRY(cudaMemcpyAsync(d_X, X, sizeof(float) * N, cudaMemcpyHostToDevice, s));
   DPM_CUDA_TRY(cudaMemcpyAsync(d_Y, Y, sizeof(float) * N, cudaMemcpyHostToDevice, s));
   DisperseArgs a{d_begin, d_r, d_L, d_X, d_Y, d_count, d_nb, d_nn, d_inner};
-  const size_t smem = sizeof(float) * 5 * (size_t)nmax;
+  // positions, starts, radii, U terms and their counts of the largest system
+  const size_t smem = sizeof(float) * (5 + kDispTerms + 1) * (size_t)nmax;
   DPM_CUDA_TRY(cudaFuncSetAttribute(k_disperse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)std::max<size_t>(smem, 1)));
+                                    (int)smem));
   k_disperse<<<nsystems, kDispThreads, smem, s>>>(a);
   DPM_CUDA_TRY(cudaGetLastError());
   DPM_CUDA_TRY(cudaMemcpyAsync(X, d_X, sizeof(float) * N, cudaMemcpyDeviceToHost, s));

@@ -76,6 +76,7 @@ struct dpm2d_batch {
   std::vector<unsigned> nv;
   std::vector<uint32_t> voff;
   std::vector<Cell2D> h_cells;
+  std::vector<float> h_Ka, h_Kl;  // spring constants as given (for the energy)
   std::vector<Tissue2D> h_tissues;
   bool cells_set = false, tissues_set = false, uploaded = false;
 
@@ -314,6 +315,8 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     if (off > (1L << 31) - 1) return fail(DPM_ECAPACITY, "too many vertices");
     b->nverts = off;
     b->h_cells.resize(total_cells);
+    b->h_Ka.assign(total_cells, 0.0f);
+    b->h_Kl.assign(total_cells, 0.0f);
     b->h_tissues.resize(ntissues);
     int cb = 0;
     for (int t = 0; t < ntissues; ++t) {
@@ -395,6 +398,8 @@ int dpm2d_set_cells(dpm2d_batch *b, const float *Ka, const float *Kl, const floa
                     const float *a0, const float *l0, const float *r0) {
   if (int r = check_batch(b)) return r;
   if (!Ka || !Kl || !Kb || !a0 || !l0 || !r0) return fail(DPM_EINVAL, "null parameter array");
+  b->h_Ka.assign(Ka, Ka + b->ncells);
+  b->h_Kl.assign(Kl, Kl + b->ncells);
   for (int c = 0; c < b->ncells; ++c) {
     if (!(a0[c] > 0.0f) || !(l0[c] > 0.0f) || !(r0[c] > 0.0f))
       return fail(DPM_EINVAL, "a0, l0 and r0 must be positive");
@@ -589,6 +594,47 @@ int dpm2d_cell_areas(dpm2d_batch *b, float *area) {
                                cudaMemcpyDeviceToHost, b->stream));
   DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   for (int c = 0; c < b->ncells; ++c) area[c] = g[c].area;
+  return DPM_OK;
+}
+
+int dpm2d_diagnostics(dpm2d_batch *b, double *area, double *perimeter, double *energy,
+                      double *packing_fraction, double *shape_index) {
+  if (int r = check_batch(b)) return r;
+  if (!b->uploaded || !b->cells_set) return fail(DPM_ESTATE, "set cells and upload first");
+  cudaSetDevice(b->ctx->device);
+  DeviceArena A;
+  DPM_CUDA_TRY(A.reserve(sizeof(double4) * b->ncells));
+  double4 *d = A.take<double4>(b->ncells);
+  DPM_CUDA_TRY(launch_diag2d(b->d_cells, b->d_pos[b->cur], d, b->ncells, b->stream));
+  std::vector<double4> h(b->ncells);
+  DPM_CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(double4) * b->ncells, cudaMemcpyDeviceToHost,
+                               b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (int c = 0; c < b->ncells; ++c) {
+    const Cell2D &C = b->h_cells[c];
+    const double Ac = h[c].x, Pc = h[c].y;
+    if (area) area[c] = Ac;
+    if (perimeter) perimeter[c] = Pc;
+    if (energy) {
+      const double da = Ac / C.a0 - 1.0;
+      energy[c] = C.nv ? 0.5 * b->h_Ka[c] * da * da + 0.5 * b->h_Kl[c] * h[c].z +
+                             0.5 * C.Kb * h[c].w
+                       : 0.0;
+    }
+  }
+  for (int t = 0; t < b->ntissues; ++t) {
+    const Tissue2D &T = b->h_tissues[t];
+    double asum = 0.0, ssum = 0.0;
+    int n = 0;
+    for (int c = T.cell_begin; c < T.cell_end; ++c) {
+      if (!b->h_cells[c].nv) continue;
+      asum += h[c].x;
+      ssum += h[c].y / std::sqrt(4.0 * M_PI * h[c].x);
+      ++n;
+    }
+    if (packing_fraction) packing_fraction[t] = asum / ((double)T.L * (double)T.L);
+    if (shape_index) shape_index[t] = n ? ssum / n : 0.0;
+  }
   return DPM_OK;
 }
 
@@ -917,6 +963,8 @@ int pool2d_assign(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, cons
       C.r0 = r0[i];
       C.inv_l0 = 1.0f / l0[i];
       C.inv_2r0 = 1.0f / (2.0f * r0[i]);
+      b->h_Ka[T.cell_begin + i] = Ka[i];
+      b->h_Kl[T.cell_begin + i] = Kl[i];
       l0max = std::max(l0max, l0[i]);
       a0max = std::max(a0max, a0[i]);
       rsum += r0[i];

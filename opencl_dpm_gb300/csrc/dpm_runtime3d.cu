@@ -493,6 +493,27 @@ int dpm3d_download(dpm3d_batch *b, float *xyz, float *F) {
   return DPM_OK;
 }
 
+int dpm3d_diagnostics(dpm3d_batch *b, double *volume, double *surface_area, double *energy) {
+  if (int r = check3(b)) return r;
+  if (!b->uploaded || !b->cells_set) return fail(DPM_ESTATE, "set cells and upload first");
+  cudaSetDevice(b->ctx->device);
+  DeviceArena A;
+  DPM_CUDA_TRY(A.reserve(sizeof(double) * 3 * b->ncells));
+  double *d = A.take<double>(3 * (size_t)b->ncells);
+  DPM_CUDA_TRY(launch_diag3d(b->d_pos[b->cur][0], b->d_pos[b->cur][1], b->d_pos[b->cur][2],
+                             b->mesh, b->d_cells, d, b->ncells, b->stream));
+  std::vector<double> h(3 * (size_t)b->ncells);
+  DPM_CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
+                               b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (int c = 0; c < b->ncells; ++c) {
+    if (volume) volume[c] = h[3 * c];
+    if (surface_area) surface_area[c] = h[3 * c + 1];
+    if (energy) energy[c] = h[3 * c + 2];
+  }
+  return DPM_OK;
+}
+
 int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts) {
   if (int r = check3(b)) return r;
   if (!counts) return fail(DPM_EINVAL, "null output");
