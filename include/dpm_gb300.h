@@ -134,6 +134,19 @@ int dpm2d_diagnostics(dpm2d_batch *b, double *area, double *perimeter,
                       double *energy, double *packing_fraction,
                       double *shape_index);
 
+/* State I/O.  dpm2d_device_state returns the DEVICE addresses of the
+ * current positions and of the last step's forces (float2 per vertex, the
+ * layout of dpm2d_upload), for zero-copy views; they stay valid until the
+ * next call that steps or uploads (positions alternate between two buffers).
+ * dpm2d_save writes the batch (shape, cell and tissue constants, positions,
+ * forces) to a checkpoint file; dpm2d_open creates a batch from one, which
+ * steps on exactly as the saved batch would have (the cell lists are
+ * rebuilt; their pruning is exact).  Replaces reading Cell2D::Verticies /
+ * Forces back after CLEulerUpdate (src/Tissue2D.cpp:223-240). */
+int dpm2d_device_state(dpm2d_batch *b, void **positions, void **forces);
+int dpm2d_save(dpm2d_batch *b, const char *path);
+int dpm2d_open(dpm_ctx *ctx, const char *path, dpm2d_batch **out);
+
 /* Cell-list snapshot for host verification (see dpm2d_rebuild_now):
  * sorted bin keys and cell ids (uint32[ncells] each), per-cell neighbour
  * counts (int32[ncells]) and lists (int32[ncells*maxnb]). */
@@ -236,6 +249,14 @@ int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts);
  * + Kb sum_edges (1 - n1.n2) (project-defined; the reference has none). */
 int dpm3d_diagnostics(dpm3d_batch *b, double *volume, double *surface_area,
                       double *energy);
+/* State I/O as for 2D: device addresses of the current x, y, z (structure of
+ * arrays, cell-major) and of the last step's force components; checkpoint
+ * save and open (mesh included).  Replaces Cell3D::GetPositions /
+ * GetForces (src/cell.cpp:232-274) for device-side consumers. */
+int dpm3d_device_state(dpm3d_batch *b, void **x, void **y, void **z, void **fx,
+                       void **fy, void **fz);
+int dpm3d_save(dpm3d_batch *b, const char *path);
+int dpm3d_open(dpm_ctx *ctx, const char *path, dpm3d_batch **out);
 
 /* ---------------------------------------------------------------------- */
 /* Dispersion of cell centres                                              */

@@ -66,6 +66,12 @@ SIGNATURES = {
                            [ctypes.c_float] * 3 + [ctypes.c_int, _vp, _vp, ctypes.c_int,
                                                    ctypes.c_float, _vp]),
     "dpm2d_diagnostics": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_double)] * 5),
+    "dpm2d_device_state": (ctypes.c_int, [_vp] + [ctypes.POINTER(_vp)] * 2),
+    "dpm2d_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "dpm2d_open": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "dpm3d_device_state": (ctypes.c_int, [_vp] + [ctypes.POINTER(_vp)] * 6),
+    "dpm3d_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "dpm3d_open": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
     "dpm3d_diagnostics": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_double)] * 3),
     "dpm_disperse": (ctypes.c_int, [_vp, ctypes.c_int, _c_int_p, _c_float_p, _c_float_p,
                                     _c_float_p, _c_float_p, _c_int_p]),
@@ -138,11 +144,48 @@ def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
 
 
+class _DeviceArray:
+    """A float32 device buffer described by __cuda_array_interface__ (v3),
+    for zero-copy views (torch.as_tensor(obj, device=...)); keeps its owner
+    alive."""
+
+    def __init__(self, ptr: int, shape, owner):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4",
+                                         "data": (int(ptr), False), "version": 3,
+                                         "strides": None}
+        self._owner = owner
+
+
+def _torch_view(ptr: int, shape, owner, device: int):
+    import torch
+    return torch.as_tensor(_DeviceArray(ptr, shape, owner), device=f"cuda:{device}")
+
+
+def _ckpt_shape(path: str, dim: int):
+    """(ntissues, per-tissue cells, per-cell NV or mesh NV) from a checkpoint
+    header (the layout written by dpm2d_save / dpm3d_save)."""
+    with open(path, "rb") as f:
+        head = f.read(16)
+        if len(head) < 16 or head[:7] != b"DPMCKPT":
+            raise DPMError(1, f"{path}: not a checkpoint")
+        if dim == 2:
+            T, N = np.frombuffer(f.read(8), np.int32)
+            f.read(8)  # vertices (int64)
+            nc = np.frombuffer(f.read(4 * T), np.int32).copy()
+            nv = np.frombuffer(f.read(4 * N), np.uint32).copy()
+            return int(T), nc, nv
+        T, N, nv, nf = np.frombuffer(f.read(16), np.int32)
+        f.read(4 * 3 * int(nf))
+        nc = np.frombuffer(f.read(4 * T), np.int32).copy()
+        return int(T), nc, int(nv)
+
+
 class Context:
     """dpm_ctx: one CUDA device and stream."""
 
     def __init__(self, device: int = 0):
         self.lib = load()
+        self.device = device
         h = _vp()
         check(self.lib.dpm_ctx_create(device, ctypes.byref(h)))
         self.h = h
@@ -207,6 +250,30 @@ class Batch2D:
 
     def set_kernel_variant(self, variant: int):
         check(self.lib.dpm2d_set_kernel_variant(self.h, variant))
+
+    def device_state(self):
+        """Zero-copy torch views (nverts, 2) of the current positions and
+        the last step's forces on the device; valid until the next step or
+        upload."""
+        p, f = _vp(), _vp()
+        check(self.lib.dpm2d_device_state(self.h, ctypes.byref(p), ctypes.byref(f)))
+        return (_torch_view(p.value, (self.nverts, 2), self, self.ctx.device),
+                _torch_view(f.value, (self.nverts, 2), self, self.ctx.device))
+
+    def save(self, path: str):
+        check(self.lib.dpm2d_save(self.h, os.fsencode(path)))
+
+    @classmethod
+    def open(cls, ctx: Context, path: str) -> "Batch2D":
+        """A batch restored from a checkpoint written by save()."""
+        T, nc, nv = _ckpt_shape(path, 2)
+        h = _vp()
+        check(ctx.lib.dpm2d_open(ctx.h, os.fsencode(path), ctypes.byref(h)))
+        b = cls.__new__(cls)
+        b.ctx, b.lib, b.h = ctx, ctx.lib, h
+        b.nv = nv
+        b.ntissues, b.ncells, b.nverts = T, int(nc.sum()), int(nv.sum())
+        return b
 
     def diagnostics(self) -> dict:
         """Per cell area, perimeter, energy; per tissue packing fraction and
@@ -357,6 +424,29 @@ class Batch3D:
         f = np.empty(self.nverts, np.uint8)
         check(self.lib.dpm3d_last_winding(self.h, f.ctypes.data_as(_c_ubyte_p)))
         return f
+
+    def device_state(self):
+        """Zero-copy torch views (nverts,) of x, y, z and of the last step's
+        force components on the device; valid until the next step or
+        upload."""
+        ptrs = [_vp() for _ in range(6)]
+        check(self.lib.dpm3d_device_state(self.h, *[ctypes.byref(p) for p in ptrs]))
+        return tuple(_torch_view(p.value, (self.nverts,), self, self.ctx.device) for p in ptrs)
+
+    def save(self, path: str):
+        check(self.lib.dpm3d_save(self.h, os.fsencode(path)))
+
+    @classmethod
+    def open(cls, ctx: Context, path: str) -> "Batch3D":
+        """A batch restored from a checkpoint written by save()."""
+        T, nc, nv = _ckpt_shape(path, 3)
+        h = _vp()
+        check(ctx.lib.dpm3d_open(ctx.h, os.fsencode(path), ctypes.byref(h)))
+        b = cls.__new__(cls)
+        b.ctx, b.lib, b.h = ctx, ctx.lib, h
+        b.ntissues, b.ncells, b.nv = T, int(nc.sum()), nv
+        b.nverts = b.ncells * nv
+        return b
 
     def diagnostics(self) -> dict:
         """Per cell volume, surface area and energy (double, on the device)."""

@@ -24,6 +24,7 @@
 #include <tuple>
 #include <vector>
 
+#include "ckpt_io.hpp"
 #include "dpm2d_kernels.cuh"
 #include "dpm_common.cuh"
 #include "dpm_runtime.hpp"
@@ -573,6 +574,104 @@ int dpm2d_download(dpm2d_batch *b, float *xy, float *F) {
   DPM_CUDA_TRY(cudaStreamSynchronize(s));
   if (err & 1) return fail(DPM_ENONFINITE, "non-finite vertex positions");
   return DPM_OK;
+}
+
+int dpm2d_device_state(dpm2d_batch *b, void **positions, void **forces) {
+  if (int r = check_batch(b)) return r;
+  if (positions) *positions = b->d_pos[b->cur];
+  if (forces) *forces = b->d_force;
+  return DPM_OK;
+}
+
+int dpm2d_save(dpm2d_batch *b, const char *path) {
+  if (int r = check_batch(b)) return r;
+  if (!b->uploaded || !b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues and upload before saving");
+  if (b->serving) return fail(DPM_ESTATE, "slot pools are not saved");
+  std::vector<float> xy(2 * (size_t)b->nverts), F(2 * (size_t)b->nverts);
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(xy.data(), b->d_pos[b->cur], sizeof(float2) * b->nverts,
+                               cudaMemcpyDeviceToHost, b->stream));
+  DPM_CUDA_TRY(cudaMemcpyAsync(F.data(), b->d_force, sizeof(float2) * b->nverts,
+                               cudaMemcpyDeviceToHost, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  const int N = b->ncells, T = b->ntissues;
+  std::vector<float> col(N);
+  CkptFile f(path, "wb");
+  if (!f.open()) return fail(DPM_EINVAL, std::string("cannot write ") + (path ? path : "(null)"));
+  f.put_header(2);
+  f.put1(T);
+  f.put1(N);
+  f.put1((int64_t)b->nverts);
+  f.put(b->tissue_ncells.data(), T);
+  f.put(b->nv.data(), N);
+  f.put(b->h_Ka.data(), N);
+  f.put(b->h_Kl.data(), N);
+  for (int k = 0; k < 4; ++k) {
+    for (int c = 0; c < N; ++c) {
+      const Cell2D &C = b->h_cells[c];
+      col[c] = k == 0 ? C.Kb : k == 1 ? C.a0 : k == 2 ? C.l0 : C.r0;
+    }
+    f.put(col.data(), N);
+  }
+  for (int k = 0; k < 4; ++k)
+    for (int t = 0; t < T; ++t) {
+      const Tissue2D &U = b->h_tissues[t];
+      if (k < 3) f.put1(k == 0 ? U.L : k == 1 ? U.Kre : U.Kat);
+      else f.put1(U.pbc);
+    }
+  f.put(xy.data(), xy.size());
+  f.put(F.data(), F.size());
+  if (!f.ok() || f.close() != 0) return fail(DPM_EINVAL, std::string("write failed: ") + path);
+  return DPM_OK;
+}
+
+int dpm2d_open(dpm_ctx *ctx, const char *path, dpm2d_batch **out) {
+  if (!ctx || !out) return fail(DPM_EINVAL, "null argument");
+  CkptFile f(path, "rb");
+  if (!f.open()) return fail(DPM_EINVAL, std::string("cannot read ") + (path ? path : "(null)"));
+  if (!f.get_header(2)) return fail(DPM_EINVAL, "not a 2D checkpoint");
+  const int T = f.get1<int>(), N = f.get1<int>();
+  const int64_t V = f.get1<int64_t>();
+  if (!f.ok() || T <= 0 || N <= 0 || V <= 0 || V > (int64_t)N * kMaxNV2D)
+    return fail(DPM_EINVAL, "corrupt checkpoint header");
+  try {
+    std::vector<int> nc(T), pbc(T);
+    std::vector<unsigned> nv(N);
+    std::vector<float> Ka(N), Kl(N), Kb(N), a0(N), l0(N), r0(N), L(T), Kre(T), Kat(T);
+    std::vector<float> xy(2 * (size_t)V), F(2 * (size_t)V);
+    f.get(nc.data(), T);
+    f.get(nv.data(), N);
+    for (auto *v : {&Ka, &Kl, &Kb, &a0, &l0, &r0}) f.get(v->data(), N);
+    for (auto *v : {&L, &Kre, &Kat}) f.get(v->data(), T);
+    f.get(pbc.data(), T);
+    f.get(xy.data(), xy.size());
+    f.get(F.data(), F.size());
+    if (!f.ok()) return fail(DPM_EINVAL, "truncated checkpoint");
+    long sum_nv = 0, sum_nc = 0;
+    for (unsigned v : nv) sum_nv += v;
+    for (int c : nc) sum_nc += c;
+    if (sum_nv != V || sum_nc != N) return fail(DPM_EINVAL, "inconsistent checkpoint sizes");
+    dpm2d_batch *b = nullptr;
+    if (int r = dpm2d_create(ctx, T, nc.data(), nv.data(), &b)) return r;
+    int r = dpm2d_set_cells(b, Ka.data(), Kl.data(), Kb.data(), a0.data(), l0.data(), r0.data());
+    if (!r) r = dpm2d_set_tissues(b, L.data(), Kre.data(), Kat.data(), pbc.data());
+    if (!r) r = dpm2d_upload(b, xy.data());
+    if (!r) {
+      const cudaError_t e = cudaMemcpyAsync(b->d_force, F.data(), sizeof(float2) * V,
+                                            cudaMemcpyHostToDevice, b->stream);
+      const cudaError_t e2 = cudaStreamSynchronize(b->stream);
+      if (e != cudaSuccess || e2 != cudaSuccess) r = cuda_fail(e ? e : e2, "checkpoint forces");
+    }
+    if (r) {
+      dpm2d_destroy(b);
+      return r;
+    }
+    *out = b;
+    return DPM_OK;
+  } catch (const std::bad_alloc &) {
+    return fail(DPM_ECAPACITY, "out of host memory");
+  }
 }
 
 int dpm2d_last_contained(dpm2d_batch *b, unsigned char *flags) {

@@ -15,9 +15,11 @@
 #include <map>
 #include <memory>
 #include <new>
+#include <string>
 #include <tuple>
 #include <vector>
 
+#include "ckpt_io.hpp"
 #include "dpm3d_kernels.cuh"
 #include "dpm_common.cuh"
 #include "dpm_runtime.hpp"
@@ -41,6 +43,7 @@ struct dpm3d_batch {
   long nverts = 0;
   std::vector<Cell3D> h_cells;
   std::vector<Tissue3D> h_tissues;
+  std::vector<unsigned> h_faces;  // the mesh as given
   bool cells_set = false, tissues_set = false, uploaded = false, bend = false;
   bool serving = false; // slot pool of a server: per-tissue step budgets
   DeviceArena arena;
@@ -214,6 +217,7 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
     if (total * nv > (1L << 31) - 1) return fail(DPM_ECAPACITY, "too many vertices");
     b->ncells = (int)total;
     b->nverts = total * nv;
+    b->h_faces.assign(faces, faces + 3 * (size_t)nf);
     // mesh tables
     std::vector<uint16_t> f16(3 * (size_t)nf);
     std::vector<std::vector<std::pair<int, int>>> inc(nv);
@@ -491,6 +495,109 @@ int dpm3d_download(dpm3d_batch *b, float *xyz, float *F) {
   }
   if (err & 1) return fail(DPM_ENONFINITE, "non-finite vertex positions");
   return DPM_OK;
+}
+
+int dpm3d_device_state(dpm3d_batch *b, void **x, void **y, void **z, void **fx, void **fy,
+                       void **fz) {
+  if (int r = check3(b)) return r;
+  if (x) *x = b->d_pos[b->cur][0];
+  if (y) *y = b->d_pos[b->cur][1];
+  if (z) *z = b->d_pos[b->cur][2];
+  if (fx) *fx = b->d_f[0];
+  if (fy) *fy = b->d_f[1];
+  if (fz) *fz = b->d_f[2];
+  return DPM_OK;
+}
+
+int dpm3d_save(dpm3d_batch *b, const char *path) {
+  if (int r = check3(b)) return r;
+  if (!b->uploaded || !b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues and upload before saving");
+  if (b->serving) return fail(DPM_ESTATE, "slot pools are not saved");
+  const size_t V = (size_t)b->nverts;
+  std::vector<float> xyz(3 * V), F(3 * V);
+  if (int r = dpm3d_download(b, xyz.data(), F.data()); r && r != DPM_ENONFINITE) return r;
+  const int N = b->ncells, T = b->ntissues;
+  std::vector<float> col(N);
+  CkptFile f(path, "wb");
+  if (!f.open()) return fail(DPM_EINVAL, std::string("cannot write ") + (path ? path : "(null)"));
+  f.put_header(3);
+  f.put1(T);
+  f.put1(N);
+  f.put1(b->nv);
+  f.put1(b->nf);
+  f.put(b->h_faces.data(), b->h_faces.size());
+  for (int t = 0; t < T; ++t) f.put1(b->h_tissues[t].cell_end - b->h_tissues[t].cell_begin);
+  for (int k = 0; k < 8; ++k) {
+    for (int c = 0; c < N; ++c) {
+      const Cell3D &C = b->h_cells[c];
+      const float v[8] = {C.Kv, C.Ka, C.Ks, C.v0, C.a0, C.l0, C.Kb, C.adh};
+      col[c] = v[k];
+    }
+    f.put(col.data(), N);
+  }
+  for (int t = 0; t < T; ++t) f.put1(b->h_tissues[t].L);
+  for (int t = 0; t < T; ++t) f.put1(b->h_tissues[t].Kre);
+  for (int t = 0; t < T; ++t) f.put1(b->h_tissues[t].pbc);
+  f.put(xyz.data(), xyz.size());
+  f.put(F.data(), F.size());
+  if (!f.ok() || f.close() != 0) return fail(DPM_EINVAL, std::string("write failed: ") + path);
+  return DPM_OK;
+}
+
+int dpm3d_open(dpm_ctx *ctx, const char *path, dpm3d_batch **out) {
+  if (!ctx || !out) return fail(DPM_EINVAL, "null argument");
+  CkptFile f(path, "rb");
+  if (!f.open()) return fail(DPM_EINVAL, std::string("cannot read ") + (path ? path : "(null)"));
+  if (!f.get_header(3)) return fail(DPM_EINVAL, "not a 3D checkpoint");
+  const int T = f.get1<int>(), N = f.get1<int>(), nv = f.get1<int>(), nf = f.get1<int>();
+  if (!f.ok() || T <= 0 || N <= 0 || nv < 4 || nv > kMaxNV3D || nf < 4 || nf > 4 * kMaxNV3D)
+    return fail(DPM_EINVAL, "corrupt checkpoint header");
+  try {
+    std::vector<unsigned> faces(3 * (size_t)nf);
+    std::vector<int> nc(T), pbc(T);
+    std::vector<float> k[8], L(T), Kre(T);
+    f.get(faces.data(), faces.size());
+    f.get(nc.data(), T);
+    for (auto &v : k) {
+      v.resize(N);
+      f.get(v.data(), N);
+    }
+    f.get(L.data(), T);
+    f.get(Kre.data(), T);
+    f.get(pbc.data(), T);
+    const size_t V = (size_t)N * nv;
+    std::vector<float> xyz(3 * V), F(3 * V);
+    f.get(xyz.data(), xyz.size());
+    f.get(F.data(), F.size());
+    if (!f.ok()) return fail(DPM_EINVAL, "truncated checkpoint");
+    long sum_nc = 0;
+    for (int c : nc) sum_nc += c;
+    if (sum_nc != N) return fail(DPM_EINVAL, "inconsistent checkpoint sizes");
+    dpm3d_batch *b = nullptr;
+    if (int r = dpm3d_create(ctx, T, nc.data(), nv, nf, faces.data(), &b)) return r;
+    int r = dpm3d_set_cells(b, k[0].data(), k[1].data(), k[2].data(), k[3].data(), k[4].data(),
+                            k[5].data(), k[6].data(), k[7].data());
+    if (!r) r = dpm3d_set_tissues(b, L.data(), Kre.data(), pbc.data());
+    if (!r) r = dpm3d_upload(b, xyz.data());
+    if (!r) {
+      cudaError_t e = cudaSuccess;
+      for (int d = 0; d < 3 && e == cudaSuccess; ++d) {
+        std::vector<float> comp(V);
+        for (size_t i = 0; i < V; ++i) comp[i] = F[3 * i + d];
+        e = cudaMemcpy(b->d_f[d], comp.data(), sizeof(float) * V, cudaMemcpyHostToDevice);
+      }
+      if (e != cudaSuccess) r = cuda_fail(e, "checkpoint forces");
+    }
+    if (r) {
+      dpm3d_destroy(b);
+      return r;
+    }
+    *out = b;
+    return DPM_OK;
+  } catch (const std::bad_alloc &) {
+    return fail(DPM_ECAPACITY, "out of host memory");
+  }
 }
 
 int dpm3d_diagnostics(dpm3d_batch *b, double *volume, double *surface_area, double *energy) {
