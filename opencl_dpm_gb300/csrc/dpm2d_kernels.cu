@@ -96,14 +96,47 @@ __device__ __forceinline__ unsigned edge_crosses(float X, float Y, float pix, fl
 //    by monotone rounding that is decided exactly by the box corners.
 //  * If only x offsets can be shifted, the y test still compares the raw
 //    signs of Y - P.y, so again an odd count needs miny < Y <= maxy.
-__device__ __forceinline__ bool vertex_candidate(float X, float Y, const Geom2D &gj,
-                                                 bool near, bool far, float L) {
+//  * If y offsets can be shifted: the reference shifts an edge's y offsets d
+//    by L*round(d/L) (each endpoint by its own rounding) when an endpoint has
+//    |d| > L.  d ranges over [fl(Y - maxy), fl(Y - miny)] and round(d/L) is
+//    monotone in d; when it is one k (|k| <= 2, so L*k is exact) over the
+//    range, unshifted edges have both offsets of k's sign (no crossing) and
+//    shifted ones have offsets fl(d - kL), so a crossing needs the image
+//    level Y - kL inside the box (exactly, by the same monotone bounds), and
+//    with no x offset shifted the count is the plain test of the image point
+//    (X, Y - kL), to which the circle test applies -- with one exception for
+//    k = -1: a vertex of the ring at offset exactly -L is not shifted in an
+//    edge whose other end is not, where the image test would count a
+//    crossing; such rings are checked vertex by vertex (kCheckMinusL).
+constexpr int kNotCandidate = 0, kCandidate = 1, kCheckMinusL = 2;
+
+__device__ __forceinline__ int shifted_y_candidate(float X, float Y, const Geom2D &gj, float L) {
+  const float dlo = __fsub_rn(Y, gj.maxy), dhi = __fsub_rn(Y, gj.miny);
+  const float k = roundf(__fdiv_rn(dlo, L));
+  if (k != roundf(__fdiv_rn(dhi, L)) || k == 0.0f || fabsf(k) > 2.0f) return kCandidate;
+  const float kL = __fmul_rn(L, k);
+  if (!(__fsub_rn(dlo, kL) <= 0.0f && __fsub_rn(dhi, kL) > 0.0f)) return kNotCandidate;
+  // an x shift would tear the ring: evaluate the reference's test
+  if (__fsub_rn(X, gj.minx) > L || __fsub_rn(gj.maxx, X) > L) return kCandidate;
+  const float Ys = __fsub_rn(Y, kL);
+  const float dx = X - gj.cx, dy = Ys - gj.cy;
+  const float rm = gj.R * (1.0f + kRelMargin) +
+                   kAbsMargin * (fabsf(gj.cx) + fabsf(gj.cy) + fabsf(X) + fabsf(Y) + L);
+  const float bm = kRelMargin * (gj.maxx - gj.minx) +
+                   kAbsMargin * (fabsf(gj.minx) + fabsf(gj.maxx) + fabsf(X));
+  if (X >= gj.minx - bm && X <= gj.maxx + bm && dx * dx + dy * dy <= rm * rm) return kCandidate;
+  // left of the ring every x intercept is to the right: nothing is counted
+  return k == -1.0f && X >= gj.minx - bm ? kCheckMinusL : kNotCandidate;
+}
+
+__device__ __forceinline__ int vertex_candidate(float X, float Y, const Geom2D &gj, bool near,
+                                                bool far, float L) {
   const bool band = Y > gj.miny && Y <= gj.maxy;
   if (far) {
     const bool fy = __fsub_rn(Y, gj.miny) > L || __fsub_rn(gj.maxy, Y) > L;
-    if (fy) return true;
+    if (fy) return shifted_y_candidate(X, Y, gj, L);
     const bool fx = __fsub_rn(X, gj.minx) > L || __fsub_rn(gj.maxx, X) > L;
-    if (fx) return band;
+    if (fx) return band ? kCandidate : kNotCandidate;
   }
   if (near && band) {
     const float dx = X - gj.cx, dy = Y - gj.cy;
@@ -111,9 +144,10 @@ __device__ __forceinline__ bool vertex_candidate(float X, float Y, const Geom2D 
                      kAbsMargin * (fabsf(gj.cx) + fabsf(gj.cy) + fabsf(X) + fabsf(Y));
     const float bm = kRelMargin * (gj.maxx - gj.minx) +
                      kAbsMargin * (fabsf(gj.minx) + fabsf(gj.maxx) + fabsf(X));
-    if (X >= gj.minx - bm && X <= gj.maxx + bm && dx * dx + dy * dy <= rm * rm) return true;
+    if (X >= gj.minx - bm && X <= gj.maxx + bm && dx * dx + dy * dy <= rm * rm)
+      return kCandidate;
   }
-  return false;
+  return kNotCandidate;
 }
 
 __device__ __forceinline__ void normalize2(float x, float y, float &ox, float &oy) {
@@ -167,7 +201,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // Per cell: |area| (shoelace), perimeter, sum over edges of (l/l0 - 1)^2 and
 // sum over vertices of |s_i|^2, s_i = (x_{i+1} - x_i) - (x_i - x_{i-1}).
 __global__ void __launch_bounds__(kGeomWarps * 32)
-    k2d_diag(const Cell2D *__restrict__ cells, const float2 *__restrict__ pos, double4 *out,
+    k2d_diag(const Cell2D *__restrict__ cells, const float2 *__restrict__ pos, Diag2D *out,
              int ncells) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * kGeomWarps + w;
@@ -175,7 +209,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32)
   const Cell2D cp = cells[c];
   const int n = (int)cp.nv;
   if (n == 0) {
-    if (lane == 0) out[c] = make_double4(0.0, 0.0, 0.0, 0.0);
+    if (lane == 0) out[c] = Diag2D{0.0, 0.0, 0.0, 0.0};
     return;
   }
   const float2 *p = pos + cp.voff;
@@ -195,7 +229,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32)
   P = warp_sum_d(P);
   Ul = warp_sum_d(Ul);
   Ub = warp_sum_d(Ub);
-  if (lane == 0) out[c] = make_double4(fabs(0.5 * A), P, Ul, Ub);
+  if (lane == 0) out[c] = Diag2D{fabs(0.5 * A), P, Ul, Ub};
 }
 
 // ---------------------------------------------------------------------------
@@ -590,16 +624,17 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     const float mm = kRelMargin * (gi.R + gj.R) +
                      kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) + fabsf(gj.cx) + fabsf(gj.cy));
 
-    unsigned cm[S], am[S];
-    bool anyc = false, anya = false;
+    unsigned cm[S], am[S], xm[S];
+    bool anyc = false, anya = false, anyx = false;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      cm[s] = am[s] = 0u;
+      cm[s] = am[s] = xm[s] = 0u;
       if (32 * s >= n) continue;  // empty slot (uniform over the warp)
       const int k = lane + 32 * s;
-      bool cand = false, ac = false;
+      int code = kNotCandidate;
+      bool ac = false;
       if (k < n) {
-        if (!sf[k]) cand = vertex_candidate(vx[s], vy[s], gj, near, far, L);
+        if (!sf[k]) code = vertex_candidate(vx[s], vy[s], gj, near, far, L);
         if (attp) {
           float ex = gj.cx - vx[s], ey = gj.cy - vy[s];
           if (pbc) {
@@ -610,18 +645,45 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
           ac = ex * ex + ey * ey <= ra * ra;
         }
       }
-      cm[s] = __ballot_sync(kFull, cand);
+      cm[s] = __ballot_sync(kFull, code == kCandidate);
+      xm[s] = __ballot_sync(kFull, code == kCheckMinusL);
       anyc |= cm[s] != 0u;
+      anyx |= xm[s] != 0u;
       if (att) {
         am[s] = __ballot_sync(kFull, ac);
         anya |= am[s] != 0u;
       }
     }
-    if (!anyc && !anya) continue;
-
+    if (!anyc && !anya && !anyx) continue;
     const uint4 jr = *reinterpret_cast<const uint4 *>(a.cells + j);
     const int nj = (int)jr.y;
     const float2 *pj = a.pos_in + jr.x;
+    if (anyx) {
+      // a vertex of the neighbour at y offset exactly -L makes it a candidate
+      float py[S];
+#pragma unroll
+      for (int s2 = 0; s2 < S; ++s2) {
+        const int e = lane + 32 * s2;
+        py[s2] = e < nj ? pj[e].y : 0.0f;
+      }
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        unsigned msk = xm[s];
+        while (msk) {
+          const int l = __ffs(msk) - 1;
+          msk &= msk - 1u;
+          const float Y = __shfl_sync(kFull, vy[s], l);
+          bool hit = false;
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2)
+            hit |= lane + 32 * s2 < nj && __fsub_rn(Y, py[s2]) == -L;
+          if (__ballot_sync(kFull, hit)) cm[s] |= 1u << l;
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) anyc |= cm[s] != 0u;
+    if (!anyc && !anya) continue;
 
     if (anya) {
       // stage the neighbour's ring for the per-vertex attraction loops
@@ -848,7 +910,7 @@ cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_diag2d(const Cell2D *cells, const float2 *pos, double4 *out, int ncells,
+cudaError_t launch_diag2d(const Cell2D *cells, const float2 *pos, Diag2D *out, int ncells,
                           cudaStream_t s) {
   const int grid = (ncells + kGeomWarps - 1) / kGeomWarps;
   k2d_diag<<<grid, kGeomWarps * 32, 0, s>>>(cells, pos, out, ncells);

@@ -49,7 +49,10 @@ cudaError_t launch_geom2d(const Cell2D *cells, const float2 *pos, Geom2D *geom,
                           int ncells, int maxnv, cudaStream_t s);
 // Per-cell diagnostics in double: (|area|, perimeter, sum (l/l0-1)^2,
 // sum |s_i|^2) of the ring at pos.
-cudaError_t launch_diag2d(const Cell2D *cells, const float2 *pos, double4 *out, int ncells,
+struct Diag2D {
+  double area, perim, ul, ub;
+};
+cudaError_t launch_diag2d(const Cell2D *cells, const float2 *pos, Diag2D *out, int ncells,
                           cudaStream_t s);
 // Per-tissue bin sizes and per-cell bin keys (one block per tissue).
 cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);

@@ -702,22 +702,22 @@ int dpm2d_diagnostics(dpm2d_batch *b, double *area, double *perimeter, double *e
   if (!b->uploaded || !b->cells_set) return fail(DPM_ESTATE, "set cells and upload first");
   cudaSetDevice(b->ctx->device);
   DeviceArena A;
-  DPM_CUDA_TRY(A.reserve(sizeof(double4) * b->ncells));
-  double4 *d = A.take<double4>(b->ncells);
+  DPM_CUDA_TRY(A.reserve(sizeof(Diag2D) * b->ncells));
+  Diag2D *d = A.take<Diag2D>(b->ncells);
   DPM_CUDA_TRY(launch_diag2d(b->d_cells, b->d_pos[b->cur], d, b->ncells, b->stream));
-  std::vector<double4> h(b->ncells);
-  DPM_CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(double4) * b->ncells, cudaMemcpyDeviceToHost,
+  std::vector<Diag2D> h(b->ncells);
+  DPM_CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(Diag2D) * b->ncells, cudaMemcpyDeviceToHost,
                                b->stream));
   DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   for (int c = 0; c < b->ncells; ++c) {
     const Cell2D &C = b->h_cells[c];
-    const double Ac = h[c].x, Pc = h[c].y;
+    const double Ac = h[c].area, Pc = h[c].perim;
     if (area) area[c] = Ac;
     if (perimeter) perimeter[c] = Pc;
     if (energy) {
       const double da = Ac / C.a0 - 1.0;
-      energy[c] = C.nv ? 0.5 * b->h_Ka[c] * da * da + 0.5 * b->h_Kl[c] * h[c].z +
-                             0.5 * C.Kb * h[c].w
+      energy[c] = C.nv ? 0.5 * b->h_Ka[c] * da * da + 0.5 * b->h_Kl[c] * h[c].ul +
+                             0.5 * C.Kb * h[c].ub
                        : 0.0;
     }
   }
@@ -727,8 +727,8 @@ int dpm2d_diagnostics(dpm2d_batch *b, double *area, double *perimeter, double *e
     int n = 0;
     for (int c = T.cell_begin; c < T.cell_end; ++c) {
       if (!b->h_cells[c].nv) continue;
-      asum += h[c].x;
-      ssum += h[c].y / std::sqrt(4.0 * M_PI * h[c].x);
+      asum += h[c].area;
+      ssum += h[c].perim / std::sqrt(4.0 * M_PI * h[c].area);
       ++n;
     }
     if (packing_fraction) packing_fraction[t] = asum / ((double)T.L * (double)T.L);
