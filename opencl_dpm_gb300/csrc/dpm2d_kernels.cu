@@ -107,8 +107,18 @@ __device__ __forceinline__ unsigned edge_crosses(float X, float Y, float pix, fl
 //    (X, Y - kL), to which the circle test applies -- with one exception for
 //    k = -1: a vertex of the ring at offset exactly -L is not shifted in an
 //    edge whose other end is not, where the image test would count a
-//    crossing; such rings are checked vertex by vertex (kCheckMinusL).
-constexpr int kNotCandidate = 0, kCandidate = 1, kCheckMinusL = 2;
+//    crossing.  Such points are kCheckY: candidates only if a ring vertex
+//    lies within a few ulps of Y + L.
+//  * If only x offsets can be shifted and the point is right of the ring by
+//    more than L somewhere (but less than 1.5 L, and right of every vertex
+//    by L/4), every offset after the reference's floor shift is >= 0, and
+//    the computed x intercept r of an edge whose y signs differ exceeds the
+//    smaller end offset minus 3.2 ulp(L); so r > 0 unless a ring vertex has
+//    x offset within 8 ulp(L) of L, and the count is the number of sign
+//    changes around the ring, even.  Such points are kCheckX.
+//    (Left of the ring by more than L, the floor shift tears the ring and
+//    the count can be odd: those points are evaluated.)
+constexpr int kNotCandidate = 0, kCandidate = 1, kCheckY = 2, kCheckX = 3;
 
 __device__ __forceinline__ int shifted_y_candidate(float X, float Y, const Geom2D &gj, float L) {
   const float dlo = __fsub_rn(Y, gj.maxy), dhi = __fsub_rn(Y, gj.miny);
@@ -126,7 +136,7 @@ __device__ __forceinline__ int shifted_y_candidate(float X, float Y, const Geom2
                    kAbsMargin * (fabsf(gj.minx) + fabsf(gj.maxx) + fabsf(X));
   if (X >= gj.minx - bm && X <= gj.maxx + bm && dx * dx + dy * dy <= rm * rm) return kCandidate;
   // left of the ring every x intercept is to the right: nothing is counted
-  return k == -1.0f && X >= gj.minx - bm ? kCheckMinusL : kNotCandidate;
+  return k == -1.0f && X >= gj.minx - bm ? kCheckY : kNotCandidate;
 }
 
 __device__ __forceinline__ int vertex_candidate(float X, float Y, const Geom2D &gj, bool near,
@@ -135,8 +145,12 @@ __device__ __forceinline__ int vertex_candidate(float X, float Y, const Geom2D &
   if (far) {
     const bool fy = __fsub_rn(Y, gj.miny) > L || __fsub_rn(gj.maxy, Y) > L;
     if (fy) return shifted_y_candidate(X, Y, gj, L);
-    const bool fx = __fsub_rn(X, gj.minx) > L || __fsub_rn(gj.maxx, X) > L;
-    if (fx) return band ? kCandidate : kNotCandidate;
+    if (__fsub_rn(gj.maxx, X) > L) return band ? kCandidate : kNotCandidate;
+    const float xr = __fsub_rn(X, gj.minx);
+    if (xr > L) {
+      if (!band) return kNotCandidate;
+      return __fsub_rn(X, gj.maxx) > 0.25f * L && xr < 1.5f * L ? kCheckX : kCandidate;
+    }
   }
   if (near && band) {
     const float dx = X - gj.cx, dy = Y - gj.cy;
@@ -624,17 +638,18 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     const float mm = kRelMargin * (gi.R + gj.R) +
                      kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) + fabsf(gj.cx) + fabsf(gj.cy));
 
-    unsigned cm[S], am[S], xm[S];
+    unsigned cm[S], am[S];
+    int code[S];
     bool anyc = false, anya = false, anyx = false;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
-      cm[s] = am[s] = xm[s] = 0u;
+      cm[s] = am[s] = 0u;
+      code[s] = kNotCandidate;
       if (32 * s >= n) continue;  // empty slot (uniform over the warp)
       const int k = lane + 32 * s;
-      int code = kNotCandidate;
       bool ac = false;
       if (k < n) {
-        if (!sf[k]) code = vertex_candidate(vx[s], vy[s], gj, near, far, L);
+        if (!sf[k]) code[s] = vertex_candidate(vx[s], vy[s], gj, near, far, L);
         if (attp) {
           float ex = gj.cx - vx[s], ey = gj.cy - vy[s];
           if (pbc) {
@@ -645,10 +660,9 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
           ac = ex * ex + ey * ey <= ra * ra;
         }
       }
-      cm[s] = __ballot_sync(kFull, code == kCandidate);
-      xm[s] = __ballot_sync(kFull, code == kCheckMinusL);
+      cm[s] = __ballot_sync(kFull, code[s] == kCandidate);
       anyc |= cm[s] != 0u;
-      anyx |= xm[s] != 0u;
+      anyx |= __any_sync(kFull, code[s] >= kCheckY);
       if (att) {
         am[s] = __ballot_sync(kFull, ac);
         anya |= am[s] != 0u;
@@ -659,19 +673,25 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     const int nj = (int)jr.y;
     const float2 *pj = a.pos_in + jr.x;
     if (anyx) {
-      // a vertex of the neighbour at y offset exactly -L makes it a candidate
-      float py[S];
+      // kCheckY points are candidates only if a ring vertex has y offset
+      // exactly -L; kCheckX points only if one has x offset within 8 ulp(L)
+      // of L.  One point at a time, the lanes scan the ring.
+      const float win = 8.0f * __int_as_float(__float_as_int(L) & 0x7f800000) * 0x1p-23f;
+      float px[S], py[S];
 #pragma unroll
       for (int s2 = 0; s2 < S; ++s2) {
         const int e = lane + 32 * s2;
-        py[s2] = e < nj ? pj[e].y : 0.0f;
+        const float2 p = e < nj ? pj[e] : make_float2(0.0f, 0.0f);
+        px[s2] = p.x;
+        py[s2] = p.y;
       }
 #pragma unroll
       for (int s = 0; s < S; ++s) {
-        unsigned msk = xm[s];
-        while (msk) {
-          const int l = __ffs(msk) - 1;
-          msk &= msk - 1u;
+        unsigned my = __ballot_sync(kFull, code[s] == kCheckY);
+        unsigned mx = __ballot_sync(kFull, code[s] == kCheckX);
+        while (my) {
+          const int l = __ffs(my) - 1;
+          my &= my - 1u;
           const float Y = __shfl_sync(kFull, vy[s], l);
           bool hit = false;
 #pragma unroll
@@ -679,11 +699,20 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
             hit |= lane + 32 * s2 < nj && __fsub_rn(Y, py[s2]) == -L;
           if (__ballot_sync(kFull, hit)) cm[s] |= 1u << l;
         }
-      }
-    }
+        while (mx) {
+          const int l = __ffs(mx) - 1;
+          mx &= mx - 1u;
+          const float X = __shfl_sync(kFull, vx[s], l);
+          bool hit = false;
 #pragma unroll
-    for (int s = 0; s < S; ++s) anyc |= cm[s] != 0u;
-    if (!anyc && !anya) continue;
+          for (int s2 = 0; s2 < S; ++s2)
+            hit |= lane + 32 * s2 < nj && fabsf(__fsub_rn(__fsub_rn(X, px[s2]), L)) <= win;
+          if (__ballot_sync(kFull, hit)) cm[s] |= 1u << l;
+        }
+        anyc |= cm[s] != 0u;
+      }
+      if (!anyc && !anya) continue;
+    }
 
     if (anya) {
       // stage the neighbour's ring for the per-vertex attraction loops
