@@ -580,11 +580,22 @@ def run_served(ctx, nreq, seed=77):
     vs, _ = srv.stats()
     srv.close()
     n2 = sum(1 for t in reqs if t["dim"] == 2)
+    dims = np.array([t["dim"] for t in reqs])
+    slow = int(np.argmax(lat))
+
+    def pct(x):
+        return {"p50": round(float(np.percentile(x, 50)), 4),
+                "p99": round(float(np.percentile(x, 99)), 4)} if len(x) else None
+
     return {
         "value": round(vs / makespan, 1), "unit": UNIT,
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 4),
                       "p99": round(float(np.percentile(lat, 99)), 4),
-                      "max": round(float(lat.max()), 4)},
+                      "max": round(float(lat.max()), 4),
+                      "2d": pct(lat[dims == 2]), "3d": pct(lat[dims == 3]),
+                      "slowest": {"dim": int(dims[slow]), "vertices": int(reqs[slow]["verts"]),
+                                  "steps": int(reqs[slow]["steps"]),
+                                  "latency_s": round(float(lat[slow]), 3)}},
         "requests": nreq, "requests_2d": n2, "requests_3d": nreq - n2,
         "vertex_steps": vs, "makespan_s": round(makespan, 3), "rounds": rounds,
         "arrival_rate_per_s": round(lam, 3),

@@ -44,6 +44,8 @@ int pool2d_release(dpm2d_batch *b, int slot);
 int pool2d_sync(dpm2d_batch *b);
 size_t pool2d_bytes(const dpm2d_batch *b);
 cudaStream_t pool2d_stream(const dpm2d_batch *b);
+// Launch over slots [0, nslots) only (the server keeps occupied slots low).
+void pool2d_set_active(dpm2d_batch *b, int nslots);
 
 int pool3d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv, int nf,
                   const unsigned *faces, dpm3d_batch **out);
@@ -57,6 +59,7 @@ int pool3d_release(dpm3d_batch *b, int slot);
 int pool3d_sync(dpm3d_batch *b);
 size_t pool3d_bytes(const dpm3d_batch *b);
 cudaStream_t pool3d_stream(const dpm3d_batch *b);
+void pool3d_set_active(dpm3d_batch *b, int nslots);
 
 // One device allocation carved into 256-byte aligned arrays.  A batch owns
 // its arena; nothing else allocates on the step path.

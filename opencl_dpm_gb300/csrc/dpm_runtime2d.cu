@@ -104,7 +104,13 @@ struct dpm2d_batch {
   bool serving = false; // slot pool of a server: per-tissue step budgets
   long rebuilds = 0;
 
-  std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
+  // slot pools: launches cover the tissues [0, run_tissues) and their cells
+  // [0, run_cells) only (0: all); the server keeps occupied slots low
+  int run_tissues = 0, run_cells = 0;
+  int nc() const { return run_cells ? run_cells : ncells; }
+  int nt() const { return run_tissues ? run_tissues : ntissues; }
+
+  std::map<std::tuple<int, int, uint32_t, int, int>, cudaGraphExec_t> graphs;
 
   ~dpm2d_batch() {
     clear_graphs();
@@ -131,8 +137,8 @@ struct dpm2d_batch {
     a.nn = d_nn;
     a.nbr = d_nbr;
     a.stale = d_stale;
-    a.ncells = ncells;
-    a.ntissues = ntissues;
+    a.ncells = nc();
+    a.ntissues = nt();
     return a;
   }
 
@@ -145,7 +151,7 @@ struct dpm2d_batch {
     cudaError_t e = launch_binprep2d(a, local_bits, s);
     if (e != cudaSuccess) return e;
     bool alt = false;
-    e = radix_sort_pairs(d_keys, d_vals, d_keys_alt, d_vals_alt, ncells, key_bits,
+    e = radix_sort_pairs(d_keys, d_vals, d_keys_alt, d_vals_alt, nc(), key_bits,
                          d_sort_scratch, s, &alt);
     if (e != cudaSuccess) return e;
     sorted_in_alt = alt;
@@ -179,7 +185,7 @@ struct dpm2d_batch {
     a.stale = d_stale;
     a.err = d_err;
     a.sched = d_sched;
-    a.ncells = ncells;
+    a.ncells = nc();
     a.dt = dt;
     return a;
   }
@@ -201,7 +207,7 @@ struct dpm2d_batch {
     cudaStream_t s = stream;
     uint32_t dtbits;
     std::memcpy(&dtbits, &dt, 4);
-    auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0);
+    auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0, nc());
     auto it = graphs.find(key);
     if (it == graphs.end()) {
       cudaGraph_t g = nullptr;
@@ -989,6 +995,7 @@ int pool2d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv_max, dpm2
   dpm2d_batch *b = nullptr;
   if (int r = dpm2d_create(ctx, nslots, nc.data(), nv.data(), &b)) return r;
   b->serving = true;
+  b->occ = 3;  // dynamic schedule: empty and frozen slots cost one fetch each
   // every cell starts as an empty slot; vertex storage stays strided by nv_max
   for (auto &C : b->h_cells) C.nv = 0;
   for (auto &T : b->h_tissues) {
@@ -1031,6 +1038,12 @@ int pool2d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv_max, dpm2
 
 size_t pool2d_bytes(const dpm2d_batch *b) { return b->arena.capacity(); }
 cudaStream_t pool2d_stream(const dpm2d_batch *b) { return b->stream; }
+
+void pool2d_set_active(dpm2d_batch *b, int nslots) {
+  nslots = std::max(1, std::min(nslots, b->ntissues));
+  b->run_tissues = nslots;
+  b->run_cells = b->h_tissues[nslots - 1].cell_cap;
+}
 
 int pool2d_assign(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, const float *Ka,
                   const float *Kl, const float *Kb, const float *a0, const float *l0,

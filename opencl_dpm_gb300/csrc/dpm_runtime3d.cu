@@ -62,7 +62,12 @@ struct dpm3d_batch {
   int local_bits = 1, key_bits = 1;
   int rebuild_period = 8;
   float skin_rel = 0.1f;
-  std::map<std::tuple<int, int, uint32_t, int>, cudaGraphExec_t> graphs;
+  // slot pools: launches cover the tissues [0, run_tissues) and their cells
+  // [0, run_cells) only (0: all)
+  int run_tissues = 0, run_cells = 0;
+  int nc() const { return run_cells ? run_cells : ncells; }
+  int nt() const { return run_tissues ? run_tissues : ntissues; }
+  std::map<std::tuple<int, int, uint32_t, int, int>, cudaGraphExec_t> graphs;
 
   ~dpm3d_batch() {
     clear_graphs();
@@ -99,13 +104,13 @@ struct dpm3d_batch {
     a.nn = d_nn;
     a.nbr = d_nbr;
     a.stale = d_stale;
-    a.ncells = ncells;
-    a.ntissues = ntissues;
+    a.ncells = nc();
+    a.ntissues = nt();
     a.block_len = block_len;
     cudaError_t e = launch_binprep3d(a, local_bits, s);
     if (e != cudaSuccess) return e;
     bool alt = false;
-    e = radix_sort_pairs(d_keys, d_vals, d_keys_alt, d_vals_alt, ncells, key_bits, d_scratch, s,
+    e = radix_sort_pairs(d_keys, d_vals, d_keys_alt, d_vals_alt, nc(), key_bits, d_scratch, s,
                          &alt);
     if (e != cudaSuccess) return e;
     a.sorted_keys = alt ? d_keys_alt : d_keys;
@@ -138,7 +143,7 @@ struct dpm3d_batch {
     a.nbr = d_nbr;
     a.stale = d_stale;
     a.err = d_err;
-    a.ncells = ncells;
+    a.ncells = nc();
     a.dt = dt;
     a.bend = bend ? 1 : 0;
     return a;
@@ -160,7 +165,7 @@ struct dpm3d_batch {
     cudaStream_t s = stream;
     uint32_t dtbits;
     std::memcpy(&dtbits, &dt, 4);
-    auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0);
+    auto key = std::make_tuple(len, cur, dtbits, last ? 1 : 0, nc());
     auto it = graphs.find(key);
     if (it == graphs.end()) {
       cudaGraph_t g = nullptr;
@@ -705,6 +710,12 @@ int pool3d_create(dpm_ctx *ctx, int nslots, int cells_per_slot, int nv, int nf,
 
 size_t pool3d_bytes(const dpm3d_batch *b) { return b->arena.capacity(); }
 cudaStream_t pool3d_stream(const dpm3d_batch *b) { return b->stream; }
+
+void pool3d_set_active(dpm3d_batch *b, int nslots) {
+  nslots = std::max(1, std::min(nslots, b->ntissues));
+  b->run_tissues = nslots;
+  b->run_cells = b->h_tissues[nslots - 1].cell_cap;
+}
 
 int pool3d_assign(dpm3d_batch *b, int slot, int ncells, const float *Kv, const float *Ka,
                   const float *Ks, const float *v0, const float *a0, const float *l0,

@@ -383,6 +383,11 @@ int dpm_serve_step(dpm_server *s, int *active, int *waiting, int *finished) {
     int inflight = 0;
     for (auto &P : s->pools) {
       if (!P.busy && P.active) {
+        // launch over the slots up to the highest occupied one
+        int hi = (int)P.slots.size();
+        while (hi > 0 && !P.slots[hi - 1]) --hi;
+        if (P.b2) pool2d_set_active(P.b2, hi);
+        else pool3d_set_active(P.b3, hi);
         const int rc =
             P.b2 ? pool2d_run(P.b2, s->chunk, P.dt) : pool3d_run(P.b3, s->chunk, P.dt);
         if (rc) return rc;
