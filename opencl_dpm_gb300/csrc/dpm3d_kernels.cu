@@ -121,22 +121,26 @@ __device__ __forceinline__ float winding_reach(const Geom3D &g) {
   return g.R + 1.05f * g.emax;
 }
 
-// Per-warp bit mask of a neighbour's vertices near the point under test.
+// Per-warp bit mask of a neighbour's vertices near the point under test,
+// and the list of their ids (when they are at most kNearList).
 constexpr int kNearWords = (kMaxNV3D + 31) / 32;
+constexpr int kNearList = 32;
 
 // Shared-memory layout of k3d_step (see step3d_smem_bytes).
 struct Smem3D {
+  float4 *pb; // bounding sphere (centre, radius) of each patch of the neighbour
   float *px, *py, *pz, *fx, *fy, *fz, *qx, *qy, *qz, *red;
   float *bnx, *bny, *bnz, *bnl, *bgx, *bgy, *bgz;
-  int *ncand;
+  int *ncand, *poff;
   unsigned *near;
-  uint16_t *faces, *cand;
+  uint16_t *faces, *cand, *pvert, *nlist;
   unsigned char *wnc;
 };
 
 __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   Smem3D s;
-  float *f = reinterpret_cast<float *>(base);
+  s.pb = reinterpret_cast<float4 *>(base);
+  float *f = reinterpret_cast<float *>(s.pb + kMaxPatches3D);
   s.px = f; f += nv;
   s.py = f; f += nv;
   s.pz = f; f += nv;
@@ -162,11 +166,17 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   }
   s.ncand = reinterpret_cast<int *>(f);
   f += 4;
+  s.poff = reinterpret_cast<int *>(f);
+  f += kMaxPatches3D + 4;
   uint16_t *h = reinterpret_cast<uint16_t *>(f);
   s.faces = h;
   h += 3 * nf;
   s.cand = h;
   h += nv;
+  s.pvert = h;
+  h += nv;
+  s.nlist = h;
+  h += kWarps * kNearList;
   s.wnc = reinterpret_cast<unsigned char *>(h);
   return s;
 }
@@ -203,36 +213,110 @@ __device__ __forceinline__ bool near_bit(const unsigned *m, int i) {
 // reference's sum equals minus the sum of the dropped terms, up to the
 // rounding of the reference's own summation: only faces with a corner near
 // pt are evaluated.  Otherwise every face is summed as the reference does.
+//
+// The support and the near vertices are found patch by patch: a patch whose
+// bounding sphere lies below the separating plane with the margin, and
+// farther than the drop range from pt, cannot change either, so only the
+// vertices of the other patches are visited.
 __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, int NV, int NF,
-                                            f3 pt, f3 cj,
-                            float emax, unsigned *nearm, int lane) {
+                                            int NP, f3 pt, f3 cj, float emax, unsigned *nearm,
+                                            uint16_t *nlist, int lane) {
   const float four_pi = 4.0f * (float)M_PI;
   const f3 du = pt - cj;
   const float r = sqrtf(dot(du, du));
   bool outside = false;
+  int nnear = 0;
   if (r > 0.0f) {
     // support of the neighbour's vertices along u = (pt - cj)/|pt - cj|,
     // and the vertices within the drop range of pt
     const f3 u = du / r;
     const float dn = 1.3f * emax;
     const float dn2 = dn * dn;
+    if (lane < kNearWords) nearm[lane] = 0u;
+    bool need = false;
+    if (lane < NP) {
+      // every vertex q of the patch has (q - cj).u <= (c - cj).u + radius
+      // and |q - pt| >= |c - pt| - radius
+      const float4 b = s.pb[lane];
+      const f3 cp = mk(b.x, b.y, b.z);
+      const float B = dot(cp - cj, u) + b.w;
+      const f3 d = cp - pt;
+      need = !(r > B + 1e-5f * (1.0f + r + fabsf(B))) ||
+             !(sqrtf(dot(d, d)) > (b.w + dn) * (1.0f + 1e-5f));
+    }
+    unsigned todo = __ballot_sync(kFull, need);
+    __syncwarp();
     float h = -INFINITY;
-    for (int base = 0; base < NV; base += 32) {
-      const int k = base + lane;
+    while (todo) {
+      const int p = __ffs(todo) - 1;
+      todo &= todo - 1u;
+      const int o = s.poff[p], n = s.poff[p + 1] - o;
       bool nr = false;
-      if (k < NV) {
+      int k = 0;
+      if (lane < n) {
+        k = s.pvert[o + lane];
         const f3 q = nbv(s, k);
         h = fmaxf(h, dot(q - cj, u));
         const f3 d = q - pt;
         nr = dot(d, d) <= dn2;
       }
-      const unsigned b = __ballot_sync(kFull, nr);
-      if (lane == 0) nearm[base >> 5] = b;
+      const unsigned bal = __ballot_sync(kFull, nr);
+      if (nr) {
+        atomicOr(nearm + (k >> 5), 1u << (k & 31));
+        const int at = nnear + __popc(bal & ((1u << lane) - 1u));
+        if (at < kNearList) nlist[at] = (uint16_t)k;
+      }
+      nnear += __popc(bal);
     }
     h = warp_max(h);
-    // rounding of the dot products is far below this margin
-    outside = r > h + 1e-5f * (1.0f + r + fabsf(h));
+    // rounding of the dot products is far below this margin; with no patch
+    // visited every patch already clears it
+    outside = h == -INFINITY || r > h + 1e-5f * (1.0f + r + fabsf(h));
     __syncwarp();
+  }
+  if (outside && nnear <= kNearList) {
+    // (near vertex, incident face) pairs, 32 at a time over the lanes;
+    // each face once, at its lowest-numbered near corner
+    float sum = 0.0f;
+    int a0 = 0, e0 = 0, deg = 0;
+    if (lane < nnear) {
+      a0 = nlist[lane];
+      e0 = m.inc_off[a0];
+      deg = m.inc_off[a0 + 1] - e0;
+    }
+    int incl = deg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    const int excl = incl - deg;
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      // the last near vertex whose pairs start at or before t
+      int o = 0;
+#pragma unroll
+      for (int st = 16; st > 0; st >>= 1)
+        if (__shfl_sync(kFull, excl, o + st) <= t) o += st;
+      const int va = __shfl_sync(kFull, a0, o);
+      const int ve = __shfl_sync(kFull, e0, o) + t - __shfl_sync(kFull, excl, o);
+      if (t < total) {
+        const int f = m.inc_face[ve];
+        const int i0 = s.faces[3 * f], i1 = s.faces[3 * f + 1], i2 = s.faces[3 * f + 2];
+        int low = NV;
+        if (near_bit(nearm, i0)) low = min(low, i0);
+        if (near_bit(nearm, i1)) low = min(low, i1);
+        if (near_bit(nearm, i2)) low = min(low, i2);
+        if (low == va) {
+          float num, denom;
+          face_term(s, i0, i1, i2, pt, num, denom);
+          if (denom < 1e-8f) sum += 2.0f * atan2f(num, denom);
+        }
+      }
+    }
+    __syncwarp();
+    return -warp_sum(sum) / four_pi;
   }
   if (outside) {
     float sum = 0.0f;
@@ -270,7 +354,8 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
   return warp_sum(part) / four_pi;
 }
 
-__global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
+// Two blocks per SM by registers (64 a thread, no spills).
+__global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   extern __shared__ __align__(16) char smem3d[];
   const int c = blockIdx.x;
   const int NV = a.mesh.nv, NF = a.mesh.nf;
@@ -301,6 +386,10 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
     s.wnc[v] = 0;
   }
   for (int i = tid; i < 3 * NF; i += kThreads) s.faces[i] = a.mesh.faces[i];
+  const int NP = a.mesh.np;
+  for (int i = tid; i < NV; i += kThreads) s.pvert[i] = a.mesh.pvert[i];
+  if (tid <= NP) s.poff[tid] = a.mesh.poff[tid];
+  if (tid < 2) s.ncand[tid] = 0;
   __syncthreads();
 
   const Geom3D gi = a.geom_in[c];
@@ -429,6 +518,7 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
     const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
     const int *list = a.nbr + (size_t)c * kMaxNB3D;
     const float L = T.L;
+    int par = 0;
     for (int q = 0; q < count; ++q) {
       const int j = scan_all ? T.cell_begin + q : list[q];
       if (j == c) continue;
@@ -446,28 +536,48 @@ __global__ void __launch_bounds__(kThreads) k3d_step(Step3DArgs a) {
       const float reach = winding_reach(gj);
       const float rr = gi.R + reach + 1e-4f * (gi.R + reach) + 1e-5f * mag;
       if (!(dot(dc, dc) <= rr * rr)) continue;
-      if (tid == 0) *s.ncand = 0;
-      __syncthreads();
+      // candidate compaction and staging of the neighbour's mesh in one
+      // phase.  Two candidate counters alternate between neighbours: the
+      // one in use was zeroed during the previous neighbour's evaluation,
+      // when nobody reads it.
+      int *cnt = s.ncand + par;
       const float rj = reach * (1.0f + 1e-4f) + 1e-5f * mag;
       for (int v = tid; v < NV; v += kThreads) {
         const f3 d = vtx(s, v) - cj;
-        if (dot(d, d) <= rj * rj) s.cand[atomicAdd(s.ncand, 1)] = (uint16_t)v;
+        if (dot(d, d) <= rj * rj) s.cand[atomicAdd(cnt, 1)] = (uint16_t)v;
+      }
+      const size_t bj = (size_t)j * NV;
+      for (int k = tid; k < NV; k += kThreads) {
+        s.qx[k] = a.xin[bj + k] + shift.x;
+        s.qy[k] = a.yin[bj + k] + shift.y;
+        s.qz[k] = a.zin[bj + k] + shift.z;
+      }
+      // bounding spheres of the neighbour's patches, from the same shifted
+      // coordinates as the staged copy
+      for (int p = w; p < NP; p += kWarps) {
+        const int o = s.poff[p], n = s.poff[p + 1] - o;
+        f3 q = mk(0.f, 0.f, 0.f);
+        if (lane < n) {
+          const int k = s.pvert[o + lane];
+          q = mk(a.xin[bj + k] + shift.x, a.yin[bj + k] + shift.y, a.zin[bj + k] + shift.z);
+        }
+        const float inv = 1.0f / (float)n;
+        const f3 cp = mk(warp_sum(q.x) * inv, warp_sum(q.y) * inv, warp_sum(q.z) * inv);
+        const f3 d = q - cp;
+        const float rad = warp_max(lane < n ? sqrtf(dot(d, d)) : 0.0f);
+        if (lane == 0) s.pb[p] = make_float4(cp.x, cp.y, cp.z, rad * (1.0f + 1e-6f));
       }
       __syncthreads();
-      const int ncand = *s.ncand;
+      const int ncand = *cnt;
+      if (tid == 0) s.ncand[par ^ 1] = 0;
+      par ^= 1;
       if (ncand > 0) {
-        const size_t bj = (size_t)j * NV;
-        for (int k = tid; k < NV; k += kThreads) {
-          s.qx[k] = a.xin[bj + k] + shift.x;
-          s.qy[k] = a.yin[bj + k] + shift.y;
-          s.qz[k] = a.zin[bj + k] + shift.z;
-        }
-        __syncthreads();
         unsigned *nearm = s.near + w * kNearWords;
         for (int i = w; i < ncand; i += kWarps) {
           const int v = s.cand[i];
           const f3 pt = vtx(s, v);
-          const float wn = winding_at(s, a.mesh, NV, NF, pt, cj, gj.emax, nearm, lane);
+          const float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj.emax, nearm,
+                                      s.nlist + w * kNearList, lane);
           if (lane == 0 && !(fabsf(wn) < 1e-6f)) {
             const f3 dir = normalize(C - pt);
             const float sc = fabsf(wn) * 0.5f * T.Kre;
@@ -772,9 +882,9 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
 
 size_t step3d_smem_bytes(int nv, int nf, bool bend) {
   size_t floats = (size_t)9 * nv + 64 + (size_t)kWarps * kNearWords +
-                  (bend ? (size_t)7 * nf : 0) + 4;
-  size_t halves = (size_t)3 * nf + nv;
-  return floats * 4 + halves * 2 + (size_t)nv + 16;
+                  (bend ? (size_t)7 * nf : 0) + 4 + kMaxPatches3D + 4;
+  size_t halves = (size_t)3 * nf + 2 * (size_t)nv + (size_t)kWarps * kNearList;
+  return sizeof(float4) * kMaxPatches3D + floats * 4 + halves * 2 + (size_t)nv + 16;
 }
 
 cudaError_t prepare_step3d(int nv, int nf, bool bend) {

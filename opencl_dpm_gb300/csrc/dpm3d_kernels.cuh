@@ -13,7 +13,15 @@ struct Mesh3D {
   const uint16_t *inc_face; // [3*nf] face ids, ascending per vertex
   const uint8_t *inc_corner;// [3*nf] corner (0..2) of the vertex in that face
   const int16_t *adj;       // [nf*3] face across edge e (vertices e, e+1), -1 none
+  // Patches: groups of at most 32 vertices that are close on the surface
+  // (vertex ids pvert[poff[p] .. poff[p+1]), np <= kMaxPatches3D).
+  int np;
+  const int *poff;          // [np+1]
+  const uint16_t *pvert;    // [nv]
 };
+
+constexpr int kMaxPatches3D = 32;
+constexpr int kPatchSize3D = 32;
 
 struct Step3DArgs {
   Mesh3D mesh;

@@ -33,6 +33,67 @@ int ceil_log2l(long v) {
   while ((1L << b) < v) ++b;
   return b;
 }
+
+// Groups the mesh vertices into patches of at most kPatchSize3D vertices
+// that lie close together on the surface: seeds by farthest-point sampling
+// in edge hops, then every vertex, nearest first, joins the nearest seed
+// with room.  The step kernel bounds each patch by a sphere at the current
+// positions, so any grouping is correct; compact patches make the bounds
+// tight.  Writes offsets off[0..np] and the vertex ids grouped by patch.
+void build_patches(int nv, int nf, const unsigned *faces, std::vector<int> &off,
+                   std::vector<uint16_t> &vert) {
+  std::vector<std::vector<int>> nb(nv);
+  for (int f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) {
+      const int a = (int)faces[3 * f + k], c = (int)faces[3 * f + (k + 1) % 3];
+      nb[a].push_back(c);
+      nb[c].push_back(a);
+    }
+  const int unreached = 1 << 29;
+  auto hops = [&](int src) {
+    std::vector<int> d(nv, unreached);
+    std::vector<int> queue{src};
+    d[src] = 0;
+    for (size_t q = 0; q < queue.size(); ++q)
+      for (int w : nb[queue[q]])
+        if (d[w] == unreached) {
+          d[w] = d[queue[q]] + 1;
+          queue.push_back(w);
+        }
+    return d;
+  };
+  const int fill = kPatchSize3D - 2; // room left for the greedy assignment
+  const int np = std::min(kMaxPatches3D, (nv + fill - 1) / fill);
+  std::vector<std::vector<int>> dist{hops(0)};
+  std::vector<int> dmin = dist[0];
+  while ((int)dist.size() < np) {
+    const int s = (int)(std::max_element(dmin.begin(), dmin.end()) - dmin.begin());
+    dist.push_back(hops(s));
+    for (int v = 0; v < nv; ++v) dmin[v] = std::min(dmin[v], dist.back()[v]);
+  }
+  std::vector<int> order(nv), count(np, 0), patch(nv, 0), seeds(np);
+  for (int v = 0; v < nv; ++v) order[v] = v;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return dmin[x] < dmin[y]; });
+  for (int v : order) {
+    for (int k = 0; k < np; ++k) seeds[k] = k;
+    std::stable_sort(seeds.begin(), seeds.end(),
+                     [&](int x, int y) { return dist[x][v] < dist[y][v]; });
+    for (int k : seeds)
+      if (count[k] < kPatchSize3D) {
+        patch[v] = k;
+        ++count[k];
+        break;
+      }
+  }
+  off.assign(1, 0);
+  vert.clear();
+  for (int k = 0; k < np; ++k) {
+    if (count[k] == 0) continue;
+    for (int v = 0; v < nv; ++v)
+      if (patch[v] == k) vert.push_back((uint16_t)v);
+    off.push_back((int)vert.size());
+  }
+}
 } // namespace
 
 struct dpm3d_batch {
@@ -244,6 +305,9 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
         incc.push_back((uint8_t)p.second);
       }
     }
+    std::vector<int> poff;
+    std::vector<uint16_t> pvert;
+    build_patches(nv, nf, faces, poff, pvert);
     std::vector<int16_t> adj(3 * (size_t)nf, -1);
     {
       std::map<std::pair<unsigned, unsigned>, std::pair<int, int>> edges;
@@ -288,13 +352,16 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
                   sizeof(int16_t) * 3 * nf + sizeof(Cell3D) * N + sizeof(Tissue3D) * ntissues +
                   9 * sizeof(float) * V + V + 3 * sizeof(Geom3D) * N +
                   sizeof(int) * (N + N * kMaxNB3D + ntissues + 1) + 4 * sizeof(uint32_t) * N +
-                  radix_sort_scratch_bytes((int)N) + 64 * 256);
+                  radix_sort_scratch_bytes((int)N) + sizeof(int) * (kMaxPatches3D + 1) +
+                  sizeof(uint16_t) * nv + 64 * 256);
     if (e != cudaSuccess) return cuda_fail(e, "device allocation");
     uint16_t *d_faces = A.take<uint16_t>(3 * nf);
     int *d_off = A.take<int>(nv + 1);
     uint16_t *d_incf = A.take<uint16_t>(3 * nf);
     uint8_t *d_incc = A.take<uint8_t>(3 * nf);
     int16_t *d_adj = A.take<int16_t>(3 * nf);
+    int *d_poff = A.take<int>(poff.size());
+    uint16_t *d_pvert = A.take<uint16_t>(nv);
     b->d_cells = A.take<Cell3D>(N);
     b->d_tissues = A.take<Tissue3D>(ntissues);
     for (int p = 0; p < 2; ++p)
@@ -326,9 +393,14 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
       e = cudaMemcpyAsync(d_incc, incc.data(), incc.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d_adj, adj.data(), 2 * adj.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_poff, poff.data(), 4 * poff.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_pvert, pvert.data(), 2 * pvert.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh upload");
-    b->mesh = Mesh3D{nv, nf, d_faces, d_off, d_incf, d_incc, d_adj};
+    b->mesh = Mesh3D{nv, nf, d_faces, d_off, d_incf, d_incc, d_adj,
+                     (int)poff.size() - 1, d_poff, d_pvert};
     e = prepare_step3d(nv, nf, true);
     if (e != cudaSuccess) return cuda_fail(e, "shared-memory opt-in");
     *out = b.release();
