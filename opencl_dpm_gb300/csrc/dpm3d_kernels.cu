@@ -106,7 +106,35 @@ __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, i
   }
   g.R = sqrtf(block_max(r2, red));
   g.emax = emax;
-  g.pad0 = g.pad1 = g.pad2 = 0.0f;
+  // Inner ball.  With the centre as origin, face (a, b, c) has the triple
+  // product t = a.(b x c), whose sign is the sign of the reference's face
+  // term at the centre, and its plane lies |t| / |n| from the centre
+  // (n = (b - a) x (c - a)).  If every t has the same sign and the solid
+  // angles sum to less than 8 pi (each is at most area / plane distance^2),
+  // the mesh winds exactly once around the centre, and no face comes closer
+  // than the smallest plane distance, so the same holds in that ball.
+  float dmin = INFINITY, bound = 0.f, npos = 0.f;
+  for (int f = threadIdx.x; f < nf; f += kThreads) {
+    const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+    const f3 a = mk(px[i0] - g.cx, py[i0] - g.cy, pz[i0] - g.cz);
+    const f3 b = mk(px[i1] - g.cx, py[i1] - g.cy, pz[i1] - g.cz);
+    const f3 c = mk(px[i2] - g.cx, py[i2] - g.cy, pz[i2] - g.cz);
+    const f3 n = cross(b - a, c - a);
+    const float nl = sqrtf(dot(n, n));
+    const float t = dot(a, cross(b, c));
+    const float d = fabsf(t) / nl;  // NaN or 0 for a degenerate face
+    dmin = d > 0.0f ? fminf(dmin, d) : -1.0f;
+    bound += 0.5f * nl / (d * d);
+    npos += t > 0.0f ? 1.0f : 0.0f;
+  }
+  dmin = -block_max(-dmin, red);
+  bound = block_sum(bound, red);
+  npos = block_sum(npos, red);
+  const bool one_sign = npos == (float)nf || npos == 0.0f;
+  const bool ok = one_sign && dmin > 0.0f && bound < 8.0f * (float)M_PI * 0.999f;
+  g.rin = ok ? dmin * (1.0f - 1e-4f) : 0.0f;
+  g.wind = npos == (float)nf ? 1.0f : -1.0f;
+  g.pad0 = 0.0f;
   return g;
 }
 
@@ -199,6 +227,65 @@ __device__ __forceinline__ bool near_bit(const unsigned *m, int i) {
   return (m[i >> 5] >> (i & 31)) & 1u;
 }
 
+// Whether the plane through pt along the most outward-facing face around
+// the nearest near vertex separates pt from every staged neighbour vertex
+// (pt then lies outside the neighbour's convex hull).  Vertices are
+// visited patch by patch as in winding_at; `span` bounds |q - pt|.
+__device__ __forceinline__ bool face_plane_separates(const Smem3D &s, const Mesh3D &m, int NP,
+                                                     f3 pt, float span, const uint16_t *nlist,
+                                                     int nnear, int lane) {
+  // nearest near vertex (lowest lane on ties)
+  float dd = INFINITY;
+  int k = 0;
+  if (lane < nnear) {
+    k = nlist[lane];
+    const f3 d = nbv(s, k) - pt;
+    dd = dot(d, d);
+  }
+  const float dbest = warp_min(dd);
+  const int src = __ffs(__ballot_sync(kFull, dd == dbest)) - 1;
+  const int k0 = __shfl_sync(kFull, k, src);
+  // its incident face with the largest signed distance of pt
+  float best = -INFINITY;
+  f3 nb = mk(0.f, 0.f, 0.f);
+  for (int e = m.inc_off[k0] + lane; e < m.inc_off[k0 + 1]; e += 32) {
+    const int f = m.inc_face[e];
+    const f3 a = nbv(s, s.faces[3 * f]), b = nbv(s, s.faces[3 * f + 1]),
+             c = nbv(s, s.faces[3 * f + 2]);
+    const f3 n = cross(b - a, c - a);
+    const float l = sqrtf(dot(n, n));
+    if (l > 0.0f) {
+      const f3 nh = n / l;
+      const float sd = dot(pt - a, nh);
+      if (sd > best) {
+        best = sd;
+        nb = nh;
+      }
+    }
+  }
+  const float top = warp_max(best);
+  if (!(top > 0.0f)) return false;
+  const int win = __ffs(__ballot_sync(kFull, best == top)) - 1;
+  const f3 n = mk(__shfl_sync(kFull, nb.x, win), __shfl_sync(kFull, nb.y, win),
+                  __shfl_sync(kFull, nb.z, win));
+  // every vertex must lie below the plane by the margin
+  const float M = 1e-5f * (1.0f + span);
+  bool need = false;
+  if (lane < NP) {
+    const float4 b = s.pb[lane];
+    need = !(dot(mk(b.x, b.y, b.z) - pt, n) + b.w < -M);
+  }
+  unsigned todo = __ballot_sync(kFull, need);
+  bool bad = false;
+  while (todo) {
+    const int p = __ffs(todo) - 1;
+    todo &= todo - 1u;
+    const int o = s.poff[p], cnt = s.poff[p + 1] - o;
+    if (lane < cnt) bad |= !(dot(nbv(s, s.pvert[o + lane]) - pt, n) < -M);
+  }
+  return !__any_sync(kFull, bad);
+}
+
 // The reference's winding number of point pt with respect to the staged
 // neighbour mesh (s.q*), as the sum over its faces of 2 atan2(num, denom) /
 // 4 pi, leaving out faces with denom < 1e-8.  One warp; every lane returns
@@ -219,12 +306,13 @@ __device__ __forceinline__ bool near_bit(const unsigned *m, int i) {
 // farther than the drop range from pt, cannot change either, so only the
 // vertices of the other patches are visited.
 __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, int NV, int NF,
-                                            int NP, f3 pt, f3 cj, float emax, unsigned *nearm,
-                                            uint16_t *nlist, int lane) {
+                                            int NP, f3 pt, f3 cj, const Geom3D &gj,
+                                            unsigned *nearm, uint16_t *nlist, int lane) {
   const float four_pi = 4.0f * (float)M_PI;
+  const float emax = gj.emax;
   const f3 du = pt - cj;
   const float r = sqrtf(dot(du, du));
-  bool outside = false;
+  bool outside = false, inside = false;
   int nnear = 0;
   if (r > 0.0f) {
     // support of the neighbour's vertices along u = (pt - cj)/|pt - cj|,
@@ -273,8 +361,18 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
     // visited every patch already clears it
     outside = h == -INFINITY || r > h + 1e-5f * (1.0f + r + fabsf(h));
     __syncwarp();
+    if (!outside && nnear <= kNearList) {
+      const float mag = fabsf(pt.x) + fabsf(pt.y) + fabsf(pt.z) + fabsf(cj.x) + fabsf(cj.y) +
+                        fabsf(cj.z);
+      // inside the neighbour's inner ball: the mesh winds gj.wind times
+      // around pt (the staged vertices differ from the neighbour's own by
+      // the rounding of the periodic shift, covered by the mag term)
+      inside = r < gj.rin - (1e-5f * (1.0f + r + gj.rin) + 1e-6f * mag);
+      if (!inside && nnear > 0)
+        outside = face_plane_separates(s, m, NP, pt, r + gj.R, nlist, nnear, lane);
+    }
   }
-  if (outside && nnear <= kNearList) {
+  if ((outside || inside) && nnear <= kNearList) {
     // (near vertex, incident face) pairs, 32 at a time over the lanes;
     // each face once, at its lowest-numbered near corner
     float sum = 0.0f;
@@ -316,7 +414,7 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
       }
     }
     __syncwarp();
-    return -warp_sum(sum) / four_pi;
+    return (inside ? gj.wind : 0.0f) - warp_sum(sum) / four_pi;
   }
   if (outside) {
     float sum = 0.0f;
@@ -576,7 +674,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
         for (int i = w; i < ncand; i += kWarps) {
           const int v = s.cand[i];
           const f3 pt = vtx(s, v);
-          const float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj.emax, nearm,
+          const float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
                                       s.nlist + w * kNearList, lane);
           if (lane == 0 && !(fabsf(wn) < 1e-6f)) {
             const f3 dir = normalize(C - pt);

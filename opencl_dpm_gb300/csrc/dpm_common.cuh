@@ -93,9 +93,12 @@ struct alignas(16) Tissue3D {
 // edge (the reference's winding sum drops faces whose denominator is below
 // 1e-8, which happens only within ~0.77 * longest edge of a face, so points
 // up to R + emax from the centre can get a non-zero winding number).
+// rin > 0: the mesh winds exactly `wind` (+1 or -1, the sign of the
+// reference's face terms) times around every point closer than rin to the
+// centre; rin = 0: no such ball is known.
 struct alignas(16) Geom3D {
   float cx, cy, cz, R;
-  float emax, pad0, pad1, pad2;
+  float emax, rin, wind, pad0;
 };
 constexpr int kMaxNB3D = 64;
 
