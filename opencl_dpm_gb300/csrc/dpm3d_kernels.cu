@@ -153,6 +153,10 @@ __device__ __forceinline__ float winding_reach(const Geom3D &g) {
 // and the list of their ids (when they are at most kNearList).
 constexpr int kNearWords = (kMaxNV3D + 31) / 32;
 constexpr int kNearList = 32;
+// Candidates whose winding number needs the sum over every face are summed
+// by the whole block after the neighbour's other candidates, up to kDefer
+// of them (more are summed by their warp).
+constexpr int kDefer = 64;
 
 // Shared-memory layout of k3d_step (see step3d_smem_bytes).
 struct Smem3D {
@@ -161,7 +165,8 @@ struct Smem3D {
   float *bnx, *bny, *bnz, *bnl, *bgx, *bgy, *bgz;
   int *ncand, *poff;
   unsigned *near;
-  uint16_t *faces, *cand, *pvert, *nlist;
+  uint16_t *faces, *cand, *pvert, *nlist, *defer;
+  float *terms; // [2][nf] face terms of a deferred candidate
   unsigned char *wnc;
 };
 
@@ -192,6 +197,8 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   } else {
     s.bnx = s.bny = s.bnz = s.bnl = s.bgx = s.bgy = s.bgz = nullptr;
   }
+  s.terms = f;
+  f += 2 * nf;
   s.ncand = reinterpret_cast<int *>(f);
   f += 4;
   s.poff = reinterpret_cast<int *>(f);
@@ -205,12 +212,25 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   h += nv;
   s.nlist = h;
   h += kWarps * kNearList;
+  s.defer = h;
+  h += kDefer;
   s.wnc = reinterpret_cast<unsigned char *>(h);
   return s;
 }
 
 __device__ __forceinline__ f3 vtx(const Smem3D &s, int i) { return mk(s.px[i], s.py[i], s.pz[i]); }
 __device__ __forceinline__ f3 nbv(const Smem3D &s, int i) { return mk(s.qx[i], s.qy[i], s.qz[i]); }
+
+// RepellingForces' contribution of one hit (Cell3D_Kernel.cl:299-308): the
+// vertex is pushed towards its own centre by |wn| Kc / 2.
+__device__ __forceinline__ void repel(const Smem3D &s, int v, float wn, f3 C, f3 pt, float Kre) {
+  const f3 dir = normalize(C - pt);
+  const float sc = fabsf(wn) * 0.5f * Kre;
+  s.fx[v] += sc * dir.x;
+  s.fy[v] += sc * dir.y;
+  s.fz[v] += sc * dir.z;
+  s.wnc[v] = (unsigned char)min(255, s.wnc[v] + 1);
+}
 
 // One face term of the reference's winding sum (Cell3D_Kernel.cl:281-297):
 // unit vectors from the point to the corners, the denominator of the
@@ -307,7 +327,9 @@ __device__ __forceinline__ bool face_plane_separates(const Smem3D &s, const Mesh
 // vertices of the other patches are visited.
 __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, int NV, int NF,
                                             int NP, f3 pt, f3 cj, const Geom3D &gj,
-                                            unsigned *nearm, uint16_t *nlist, int lane) {
+                                            unsigned *nearm, uint16_t *nlist, int lane,
+                                            bool may_defer, bool &deferred) {
+  deferred = false;
   const float four_pi = 4.0f * (float)M_PI;
   const float emax = gj.emax;
   const f3 du = pt - cj;
@@ -406,7 +428,16 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
         if (near_bit(nearm, i0)) low = min(low, i0);
         if (near_bit(nearm, i1)) low = min(low, i1);
         if (near_bit(nearm, i2)) low = min(low, i2);
-        if (low == va) {
+        // A face subtends at most what the disc around its centroid through
+        // its farthest corner subtends, and a disc of radius rho subtends
+        // pi steradians or more only within rho of its centre: farther
+        // away (here with a 25% margin) the reference's denominator is
+        // clearly positive and the face is kept.
+        const f3 A = nbv(s, i0), B = nbv(s, i1), Cc = nbv(s, i2);
+        const f3 g = (1.0f / 3.0f) * (A + B + Cc);
+        const f3 ga = A - g, gb = B - g, gc = Cc - g, gp = pt - g;
+        const float rho2 = fmaxf(dot(ga, ga), fmaxf(dot(gb, gb), dot(gc, gc)));
+        if (low == va && dot(gp, gp) <= 1.5625f * rho2) {
           float num, denom;
           face_term(s, i0, i1, i2, pt, num, denom);
           if (denom < 1e-8f) sum += 2.0f * atan2f(num, denom);
@@ -441,6 +472,11 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
     }
     __syncwarp();
     return -warp_sum(sum) / four_pi;
+  }
+  if (may_defer) {
+    // the block sums it after this neighbour's candidates
+    deferred = true;
+    return 0.0f;
   }
   float part = 0.0f;
   for (int f = lane; f < NF; f += 32) {
@@ -487,7 +523,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   const int NP = a.mesh.np;
   for (int i = tid; i < NV; i += kThreads) s.pvert[i] = a.mesh.pvert[i];
   if (tid <= NP) s.poff[tid] = a.mesh.poff[tid];
-  if (tid < 2) s.ncand[tid] = 0;
+  if (tid < 3) s.ncand[tid] = 0;
   __syncthreads();
 
   const Geom3D gi = a.geom_in[c];
@@ -674,21 +710,52 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
         for (int i = w; i < ncand; i += kWarps) {
           const int v = s.cand[i];
           const f3 pt = vtx(s, v);
-          const float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                                      s.nlist + w * kNearList, lane);
-          if (lane == 0 && !(fabsf(wn) < 1e-6f)) {
-            const f3 dir = normalize(C - pt);
-            const float sc = fabsf(wn) * 0.5f * T.Kre;
-            s.fx[v] += sc * dir.x;
-            s.fy[v] += sc * dir.y;
-            s.fz[v] += sc * dir.z;
-            s.wnc[v] = (unsigned char)min(255, s.wnc[v] + 1);
+          bool deferred;
+          float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
+                                s.nlist + w * kNearList, lane, true, deferred);
+          if (deferred) {
+            int slot = 0;
+            if (lane == 0) slot = atomicAdd(s.ncand + 2, 1);
+            slot = __shfl_sync(kFull, slot, 0);
+            if (slot < kDefer) {
+              if (lane == 0) s.defer[slot] = (uint16_t)v;
+              continue;
+            }
+            wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
+                            s.nlist + w * kNearList, lane, false, deferred);
           }
+          if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
           __syncwarp();
         }
       }
       __syncthreads();
+      // the deferred candidates, one after the other: the block evaluates
+      // the face terms into a buffer, then one warp adds them up in the
+      // order of the warp-level sum (lane l: faces l, l + 32, ...; then
+      // the butterfly), so the result is the one that warp would give;
+      // two buffers let that warp add while the block evaluates the next
+      const int nd = min(s.ncand[2], kDefer);
+      for (int d = 0; d < nd; ++d) {
+        float *tb = s.terms + (d & 1) * NF;
+        const int v = s.defer[d];
+        const f3 pt = vtx(s, v);
+        for (int f = tid; f < NF; f += kThreads) {
+          float num, denom;
+          face_term(s, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num, denom);
+          tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
+        }
+        __syncthreads();
+        if (tid == 0 && d == nd - 1) s.ncand[2] = 0;
+        if (w == d % kWarps) {
+          float part = 0.0f;
+          for (int f = lane; f < NF; f += 32) part += tb[f];
+          const float wn = warp_sum(part) / (4.0f * (float)M_PI);
+          if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+        }
+      }
     }
+    // the last deferred sum's force lands after the loop's last barrier
+    __syncthreads();
   }
 
   // EulerPosition (Cell3D_Kernel.cl:371-381) and outputs
@@ -980,8 +1047,9 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
 
 size_t step3d_smem_bytes(int nv, int nf, bool bend) {
   size_t floats = (size_t)9 * nv + 64 + (size_t)kWarps * kNearWords +
-                  (bend ? (size_t)7 * nf : 0) + 4 + kMaxPatches3D + 4;
-  size_t halves = (size_t)3 * nf + 2 * (size_t)nv + (size_t)kWarps * kNearList;
+                  (bend ? (size_t)7 * nf : 0) + (size_t)2 * nf + 4 +
+                  kMaxPatches3D + 4;
+  size_t halves = (size_t)3 * nf + 2 * (size_t)nv + (size_t)kWarps * kNearList + kDefer;
   return sizeof(float4) * kMaxPatches3D + floats * 4 + halves * 2 + (size_t)nv + 16;
 }
 
