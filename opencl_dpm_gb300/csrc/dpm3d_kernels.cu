@@ -167,10 +167,16 @@ struct Smem3D {
   unsigned *near;
   uint16_t *faces, *cand, *pvert, *nlist, *defer;
   float *terms; // [2][nf] face terms of a deferred candidate
+  float *ex, *ey, *ez, *eL; // unit vector (lower id -> higher id) and length of each edge
   unsigned char *wnc;
 };
 
-__device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
+__host__ __device__ __forceinline__ int q_region(int nv, int nf, int ne) {
+  const int a = 3 * nv + 2 * nf, b = 4 * ne;
+  return a > b ? a : b;
+}
+
+__device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool bend) {
   Smem3D s;
   s.pb = reinterpret_cast<float4 *>(base);
   float *f = reinterpret_cast<float *>(s.pb + kMaxPatches3D);
@@ -180,9 +186,18 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   s.fx = f; f += nv;
   s.fy = f; f += nv;
   s.fz = f; f += nv;
-  s.qx = f; f += nv;
-  s.qy = f; f += nv;
-  s.qz = f; f += nv;
+  // one region, two lives: the unit vectors and lengths of the mesh edges
+  // while the shape forces are formed, then the staged neighbour and the
+  // face terms of deferred candidates during the repulsion
+  s.qx = f;
+  s.qy = f + nv;
+  s.qz = f + 2 * nv;
+  s.terms = f + 3 * nv;
+  s.ex = f;
+  s.ey = f + ne;
+  s.ez = f + 2 * ne;
+  s.eL = f + 3 * ne;
+  f += q_region(nv, nf, ne);
   s.red = f; f += 64;
   s.near = reinterpret_cast<unsigned *>(f);
   f += kWarps * kNearWords;
@@ -197,8 +212,6 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
   } else {
     s.bnx = s.bny = s.bnz = s.bnl = s.bgx = s.bgy = s.bgz = nullptr;
   }
-  s.terms = f;
-  f += 2 * nf;
   s.ncand = reinterpret_cast<int *>(f);
   f += 4;
   s.poff = reinterpret_cast<int *>(f);
@@ -220,6 +233,12 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, bool bend) {
 
 __device__ __forceinline__ f3 vtx(const Smem3D &s, int i) { return mk(s.px[i], s.py[i], s.pz[i]); }
 __device__ __forceinline__ f3 nbv(const Smem3D &s, int i) { return mk(s.qx[i], s.qy[i], s.qz[i]); }
+// unit vector of edge id g & 0x7fff, negated when bit 15 is set
+__device__ __forceinline__ f3 edge_unit(const Smem3D &s, int g) {
+  const int i = g & 0x7fff;
+  const f3 n = mk(s.ex[i], s.ey[i], s.ez[i]);
+  return (g & 0x8000) ? mk(-n.x, -n.y, -n.z) : n;
+}
 
 // RepellingForces' contribution of one hit (Cell3D_Kernel.cl:299-308): the
 // vertex is pushed towards its own centre by |wn| Kc / 2.
@@ -494,7 +513,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   const int c = blockIdx.x;
   const int NV = a.mesh.nv, NF = a.mesh.nf;
   const bool bend_any = a.bend != 0;
-  Smem3D s = carve(smem3d, NV, NF, bend_any);
+  Smem3D s = carve(smem3d, NV, NF, a.mesh.ne, bend_any);
   const Cell3D P = a.cells[c];
   if (!P.active) return;  // an empty slot (uniform over the block)
   const Tissue3D T = a.tissues[P.tissue];
@@ -539,6 +558,19 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   const float volume = fabsf(block_sum(vpart, s.red));
   const float kvol = -P.Kv * (volume / P.v0 - 1.0f);
 
+  // edge pass of SurfaceAreaForceUpdate: every face term uses the unit
+  // vector and length of its edges, formed here once per edge
+  if (!(P.Ka < 1e-8f)) {
+    for (int e = tid; e < a.mesh.ne; e += kThreads) {
+      const f3 lv = vtx(s, a.mesh.eva[2 * e + 1]) - vtx(s, a.mesh.eva[2 * e]);
+      const float L = sqrtf(dot(lv, lv));
+      const f3 n = lv / L;
+      s.ex[e] = n.x;
+      s.ey[e] = n.y;
+      s.ez[e] = n.z;
+      s.eL[e] = L;
+    }
+  }
   // triangle bending, face pass (extension): unit normals, then G per face
   const bool bend = bend_any && P.Kb != 0.0f;
   if (bend) {
@@ -553,7 +585,9 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
       s.bnz[f] = nh.z;
       s.bnl[f] = l;
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  if (bend) {
     for (int f = tid; f < NF; f += kThreads) {
       f3 G = mk(0.f, 0.f, 0.f);
       const float l = s.bnl[f];
@@ -593,18 +627,21 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
     if (!(P.Ka < 1e-8f)) {
       for (int e = e0; e < e1; ++e) {
         const int f = a.mesh.inc_face[e], k = a.mesh.inc_corner[e];
-        const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
-                 p2 = vtx(s, s.faces[3 * f + 2]);
-        const f3 lv0 = p1 - p0, lv1 = p2 - p1, lv2 = p0 - p2;
-        const float L0 = sqrtf(dot(lv0, lv0)), L1 = sqrtf(dot(lv1, lv1)),
-                    L2 = sqrtf(dot(lv2, lv2));
+        // edge i runs from corner i to corner i+1: lv_i = p_{i+1} - p_i,
+        // L_i = |lv_i|, n_i = lv_i / L_i (from the edge pass, negated when
+        // the face runs the edge the other way)
+        const int g0 = a.mesh.fedge[3 * f], g1 = a.mesh.fedge[3 * f + 1],
+                  g2 = a.mesh.fedge[3 * f + 2];
+        const float L0 = s.eL[g0 & 0x7fff], L1 = s.eL[g1 & 0x7fff], L2 = s.eL[g2 & 0x7fff];
         if (L0 < 1e-12f || L1 < 1e-12f || L2 < 1e-12f) continue;
-        const f3 n0 = lv0 / L0, n1 = lv1 / L1, n2 = lv2 / L2;
-        const float d0 = L0 / P.l0 - 1.0f, d1 = L1 / P.l0 - 1.0f, d2 = L2 / P.l0 - 1.0f;
-        f3 g;
-        if (k == 0) g = d0 * n0 - d2 * n2;
-        else if (k == 1) g = d1 * n1 - d0 * n0;
-        else g = d2 * n2 - d1 * n1;
+        // corner k: g = d_k n_k - d_{k-1} n_{k-1}, d_i = L_i / l0 - 1
+        const int ga = k == 0 ? g0 : (k == 1 ? g1 : g2);
+        const int gb = k == 0 ? g2 : (k == 1 ? g0 : g1);
+        const float La = k == 0 ? L0 : (k == 1 ? L1 : L2);
+        const float Lb = k == 0 ? L2 : (k == 1 ? L0 : L1);
+        const f3 na = edge_unit(s, ga), nb = edge_unit(s, gb);
+        const float da = La / P.l0 - 1.0f, db = Lb / P.l0 - 1.0f;
+        const f3 g = da * na - db * nb;
         F = F + P.sa_scale * g;
       }
     }
@@ -614,8 +651,11 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
         const int f = a.mesh.inc_face[e], k = a.mesh.inc_corner[e];
         const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
                  p2 = vtx(s, s.faces[3 * f + 2]);
-        const f3 un = normalize(cross(p1 - p0, p2 - p0));
-        if (!(un.z < -0.1f)) continue;
+        // z of the unit normal (normalize's other components are unused)
+        const f3 nn = cross(p1 - p0, p2 - p0);
+        const float nl2 = dot(nn, nn);
+        const float unz = nl2 == 0.0f ? nn.z : nn.z / sqrtf(nl2);
+        if (!(unz < -0.1f)) continue;
         const f3 pos = k == 0 ? p0 : (k == 1 ? p1 : p2);
         if (pos.z < 0.0f) F.z += P.Ks * fabsf(pos.z);
         if (fabsf(pos.z) < range) {
@@ -1045,21 +1085,21 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
 
 } // namespace
 
-size_t step3d_smem_bytes(int nv, int nf, bool bend) {
-  size_t floats = (size_t)9 * nv + 64 + (size_t)kWarps * kNearWords +
-                  (bend ? (size_t)7 * nf : 0) + (size_t)2 * nf + 4 +
+size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend) {
+  size_t floats = (size_t)6 * nv + (size_t)q_region(nv, nf, ne) + 64 +
+                  (size_t)kWarps * kNearWords + (bend ? (size_t)7 * nf : 0) + 4 +
                   kMaxPatches3D + 4;
   size_t halves = (size_t)3 * nf + 2 * (size_t)nv + (size_t)kWarps * kNearList + kDefer;
   return sizeof(float4) * kMaxPatches3D + floats * 4 + halves * 2 + (size_t)nv + 16;
 }
 
-cudaError_t prepare_step3d(int nv, int nf, bool bend) {
-  const size_t bytes = step3d_smem_bytes(nv, nf, bend);
+cudaError_t prepare_step3d(int nv, int nf, int ne, bool bend) {
+  const size_t bytes = step3d_smem_bytes(nv, nf, ne, bend);
   return cudaFuncSetAttribute(k3d_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {
-  const size_t bytes = step3d_smem_bytes(a.mesh.nv, a.mesh.nf, a.bend != 0);
+  const size_t bytes = step3d_smem_bytes(a.mesh.nv, a.mesh.nf, a.mesh.ne, a.bend != 0);
   k3d_step<<<a.ncells, kThreads, bytes, s>>>(a);
   return cudaGetLastError();
 }

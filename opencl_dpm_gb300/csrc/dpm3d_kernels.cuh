@@ -18,6 +18,11 @@ struct Mesh3D {
   int np;
   const int *poff;          // [np+1]
   const uint16_t *pvert;    // [nv]
+  // Edges: endpoints (lower id first) and, per face corner k, the edge from
+  // corner k to corner k+1 (bit 15 set when it runs from the higher id).
+  int ne;
+  const uint16_t *eva;      // [2*ne]
+  const uint16_t *fedge;    // [3*nf]
 };
 
 constexpr int kMaxPatches3D = 32;
@@ -62,8 +67,8 @@ cudaError_t launch_diag3d(const float *x, const float *y, const float *z, const 
                           const Cell3D *cells, double *out, int ncells, cudaStream_t s);
 cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
-size_t step3d_smem_bytes(int nv, int nf, bool bend);
-cudaError_t prepare_step3d(int nv, int nf, bool bend);
+size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend);
+cudaError_t prepare_step3d(int nv, int nf, int ne, bool bend);
 cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s);
 
 } // namespace dpm

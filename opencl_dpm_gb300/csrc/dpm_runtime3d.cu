@@ -309,12 +309,22 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
     std::vector<uint16_t> pvert;
     build_patches(nv, nf, faces, poff, pvert);
     std::vector<int16_t> adj(3 * (size_t)nf, -1);
+    // edges: endpoints (lower id first) and the edge of each face corner
+    std::vector<uint16_t> eva, fedge(3 * (size_t)nf);
     {
       std::map<std::pair<unsigned, unsigned>, std::pair<int, int>> edges;
+      std::map<std::pair<unsigned, unsigned>, int> edge_id;
       for (int f = 0; f < nf; ++f)
         for (int e = 0; e < 3; ++e) {
           const unsigned a = faces[3 * f + e], c = faces[3 * f + (e + 1) % 3];
           auto key = std::make_pair(std::min(a, c), std::max(a, c));
+          auto id = edge_id.find(key);
+          if (id == edge_id.end()) {
+            id = edge_id.emplace(key, (int)eva.size() / 2).first;
+            eva.push_back((uint16_t)key.first);
+            eva.push_back((uint16_t)key.second);
+          }
+          fedge[3 * f + e] = (uint16_t)(id->second | (a > c ? 0x8000 : 0));
           auto it = edges.find(key);
           if (it == edges.end()) {
             edges.emplace(key, std::make_pair(f, e));
@@ -324,6 +334,7 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
           }
         }
     }
+    const int ne = (int)eva.size() / 2;
     b->h_cells.resize(total);
     b->h_tissues.resize(ntissues);
     int cb = 0;
@@ -353,7 +364,7 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
                   9 * sizeof(float) * V + V + 3 * sizeof(Geom3D) * N +
                   sizeof(int) * (N + N * kMaxNB3D + ntissues + 1) + 4 * sizeof(uint32_t) * N +
                   radix_sort_scratch_bytes((int)N) + sizeof(int) * (kMaxPatches3D + 1) +
-                  sizeof(uint16_t) * nv + 64 * 256);
+                  sizeof(uint16_t) * (nv + eva.size() + fedge.size()) + 64 * 256);
     if (e != cudaSuccess) return cuda_fail(e, "device allocation");
     uint16_t *d_faces = A.take<uint16_t>(3 * nf);
     int *d_off = A.take<int>(nv + 1);
@@ -362,6 +373,8 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
     int16_t *d_adj = A.take<int16_t>(3 * nf);
     int *d_poff = A.take<int>(poff.size());
     uint16_t *d_pvert = A.take<uint16_t>(nv);
+    uint16_t *d_eva = A.take<uint16_t>(eva.size());
+    uint16_t *d_fedge = A.take<uint16_t>(fedge.size());
     b->d_cells = A.take<Cell3D>(N);
     b->d_tissues = A.take<Tissue3D>(ntissues);
     for (int p = 0; p < 2; ++p)
@@ -397,11 +410,15 @@ int dpm3d_create(dpm_ctx *ctx, int ntissues, const int *ncells, int nv, int nf,
       e = cudaMemcpyAsync(d_poff, poff.data(), 4 * poff.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d_pvert, pvert.data(), 2 * pvert.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_eva, eva.data(), 2 * eva.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_fedge, fedge.data(), 2 * fedge.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "mesh upload");
     b->mesh = Mesh3D{nv, nf, d_faces, d_off, d_incf, d_incc, d_adj,
-                     (int)poff.size() - 1, d_poff, d_pvert};
-    e = prepare_step3d(nv, nf, true);
+                     (int)poff.size() - 1, d_poff, d_pvert, ne, d_eva, d_fedge};
+    e = prepare_step3d(nv, nf, ne, true);
     if (e != cudaSuccess) return cuda_fail(e, "shared-memory opt-in");
     *out = b.release();
     ctx_retain(ctx);
