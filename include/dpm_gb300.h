@@ -229,6 +229,12 @@ int dpm3d_set_cells(dpm3d_batch *b, const float *Kv, const float *Ka,
 /* Per-tissue constants: L, Kre (the reference's Kc), pbc. */
 int dpm3d_set_tissues(dpm3d_batch *b, const float *L, const float *Kre,
                       const int *pbc);
+/* Opt-in: the reference's AllVertAttraction kernel
+ * (shaders/Cell3D_Kernel.cl:313-364), which its own step loop
+ * (src/Tissue3D.cpp:372-445) never enqueues, run after the repulsion of
+ * every step with strength Kat[t] per tissue (0 = off, the default).  Call
+ * after dpm3d_set_cells and dpm3d_set_tissues. */
+int dpm3d_set_attraction(dpm3d_batch *b, const float *Kat);
 int dpm3d_upload(dpm3d_batch *b, const float *xyz);
 /* Replaces the step loop of src/Tissue3D.cpp:372-445. */
 int dpm3d_step(dpm3d_batch *b, int nsteps, float dt);

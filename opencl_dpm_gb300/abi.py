@@ -56,6 +56,7 @@ SIGNATURES = {
     "dpm3d_destroy": (ctypes.c_int, [_vp]),
     "dpm3d_set_cells": (ctypes.c_int, [_vp] + [_c_float_p] * 8),
     "dpm3d_set_tissues": (ctypes.c_int, [_vp, _c_float_p, _c_float_p, _c_int_p]),
+    "dpm3d_set_attraction": (ctypes.c_int, [_vp, _c_float_p]),
     "dpm3d_upload": (ctypes.c_int, [_vp, _vp]),
     "dpm3d_step": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
     "dpm3d_download": (ctypes.c_int, [_vp, _vp, _vp]),
@@ -402,6 +403,11 @@ class Batch3D:
         L, Kre = (_f32(np.broadcast_to(x, (self.ntissues,))) for x in (L, Kre))
         p = np.ascontiguousarray(np.broadcast_to(pbc, (self.ntissues,)), dtype=np.int32)
         check(self.lib.dpm3d_set_tissues(self.h, fptr(L), fptr(Kre), p.ctypes.data_as(_c_int_p)))
+
+    def set_attraction(self, Kat):
+        """Opt-in AllVertAttraction with strength Kat per tissue (0 = off)."""
+        Kat = _f32(np.broadcast_to(Kat, (self.ntissues,)))
+        check(self.lib.dpm3d_set_attraction(self.h, fptr(Kat)))
 
     def set_tuning(self, rebuild_period=0, skin_rel=0.0):
         check(self.lib.dpm3d_set_tuning(self.h, rebuild_period, skin_rel))

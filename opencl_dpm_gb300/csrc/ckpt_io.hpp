@@ -28,6 +28,11 @@ public:
   template <typename T> void get(T *p, size_t n) {
     if (ok() && n && std::fread(p, sizeof(T), n, f_) != n) ok_ = false;
   }
+  // reads n items if they are there; false (and nothing changed) at the end
+  // of the file, for optional trailing sections
+  template <typename T> bool try_get(T *p, size_t n) {
+    return ok() && n && std::fread(p, sizeof(T), n, f_) == n;
+  }
   template <typename T> T get1() {
     T v{};
     get(&v, 1);

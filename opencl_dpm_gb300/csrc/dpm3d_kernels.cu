@@ -508,6 +508,74 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
 }
 
 // Two blocks per SM by registers (64 a thread, no spills).
+// Stages cell j's vertices, shifted to the periodic image nearest this cell,
+// into s.q*, and the bounding spheres of its patches, from the same shifted
+// coordinates, into s.pb (the whole block; no barrier).
+__device__ __forceinline__ void stage_neighbour(const Smem3D &s, const Step3DArgs &a, int j,
+                                                f3 shift, int NV, int NP, int tid, int w,
+                                                int lane) {
+  const size_t bj = (size_t)j * NV;
+  for (int k = tid; k < NV; k += kThreads) {
+    s.qx[k] = a.xin[bj + k] + shift.x;
+    s.qy[k] = a.yin[bj + k] + shift.y;
+    s.qz[k] = a.zin[bj + k] + shift.z;
+  }
+  for (int p = w; p < NP; p += kWarps) {
+    const int o = s.poff[p], n = s.poff[p + 1] - o;
+    f3 q = mk(0.f, 0.f, 0.f);
+    if (lane < n) {
+      const int k = s.pvert[o + lane];
+      q = mk(a.xin[bj + k] + shift.x, a.yin[bj + k] + shift.y, a.zin[bj + k] + shift.z);
+    }
+    const float inv = 1.0f / (float)n;
+    const f3 cp = mk(warp_sum(q.x) * inv, warp_sum(q.y) * inv, warp_sum(q.z) * inv);
+    const f3 d = q - cp;
+    const float rad = warp_max(lane < n ? sqrtf(dot(d, d)) : 0.0f);
+    if (lane == 0) s.pb[p] = make_float4(cp.x, cp.y, cp.z, rad * (1.0f + 1e-6f));
+  }
+}
+
+// Shift of cell j to its periodic image nearest the centre (cx, cy, cz).
+__device__ __forceinline__ f3 image_shift(const Geom3D &gi, const Geom3D &gj, const Tissue3D &T) {
+  if (!T.pbc) return mk(0.f, 0.f, 0.f);
+  const float L = T.L;
+  return mk(__fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cx, gj.cx), L))),
+            __fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cy, gj.cy), L))),
+            __fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cz, gj.cz), L))));
+}
+
+// One ordered pair of AllVertAttraction as the reference computes it
+// (Cell3D_Kernel.cl:339-361), seen from vertex p of the cell with rest
+// length L0i: delta = q - p from the raw positions, wrapped by
+// L*round(delta/L); -tmp(L0i) from this cell's visit and +tmp'(L0j), built on
+// -delta, from the other cell's visit, each added to (fx, fy, fz) as the
+// reference's atomics add them.
+__device__ __forceinline__ void attract_pair(f3 p, f3 q, float L0i, float L0j, float Kat,
+                                             float L, bool pbc, float &fx, float &fy,
+                                             float &fz) {
+  float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+  if (pbc) {
+    dx = __fsub_rn(dx, __fmul_rn(L, roundf(__fdiv_rn(dx, L))));
+    dy = __fsub_rn(dy, __fmul_rn(L, roundf(__fdiv_rn(dy, L))));
+    dz = __fsub_rn(dz, __fmul_rn(L, roundf(__fdiv_rn(dz, L))));
+  }
+  const float dist =
+      __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+  const float k2 = __fmul_rn(Kat, 0.5f);
+  if (dist < L0i * 2.0f && dist > 1e-12f) {
+    const float t = __fmul_rn(k2, __fsub_rn(__fdiv_rn(dist, L0i), 1.0f));
+    fx = __fadd_rn(fx, -__fmul_rn(t, __fdiv_rn(dx, dist)));
+    fy = __fadd_rn(fy, -__fmul_rn(t, __fdiv_rn(dy, dist)));
+    fz = __fadd_rn(fz, -__fmul_rn(t, __fdiv_rn(dz, dist)));
+  }
+  if (dist < L0j * 2.0f && dist > 1e-12f) {
+    const float t = __fmul_rn(k2, __fsub_rn(__fdiv_rn(dist, L0j), 1.0f));
+    fx = __fadd_rn(fx, __fmul_rn(t, __fdiv_rn(-dx, dist)));
+    fy = __fadd_rn(fy, __fmul_rn(t, __fdiv_rn(-dy, dist)));
+    fz = __fadd_rn(fz, __fmul_rn(t, __fdiv_rn(-dz, dist)));
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   extern __shared__ __align__(16) char smem3d[];
   const int c = blockIdx.x;
@@ -691,18 +759,12 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
         nnc == kNbOverflow || *((volatile const int *)(a.stale + P.tissue)) != 0;
     const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
     const int *list = a.nbr + (size_t)c * kMaxNB3D;
-    const float L = T.L;
     int par = 0;
     for (int q = 0; q < count; ++q) {
       const int j = scan_all ? T.cell_begin + q : list[q];
       if (j == c) continue;
       const Geom3D gj = a.geom_in[j];
-      f3 shift = mk(0.f, 0.f, 0.f);
-      if (T.pbc) {
-        shift = mk(__fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cx, gj.cx), L))),
-                   __fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cy, gj.cy), L))),
-                   __fmul_rn(L, roundf(__fdiv_rn(__fsub_rn(gi.cz, gj.cz), L))));
-      }
+      const f3 shift = image_shift(gi, gj, T);
       const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
       const f3 dc = C - cj;
       const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
@@ -720,27 +782,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
         const f3 d = vtx(s, v) - cj;
         if (dot(d, d) <= rj * rj) s.cand[atomicAdd(cnt, 1)] = (uint16_t)v;
       }
-      const size_t bj = (size_t)j * NV;
-      for (int k = tid; k < NV; k += kThreads) {
-        s.qx[k] = a.xin[bj + k] + shift.x;
-        s.qy[k] = a.yin[bj + k] + shift.y;
-        s.qz[k] = a.zin[bj + k] + shift.z;
-      }
-      // bounding spheres of the neighbour's patches, from the same shifted
-      // coordinates as the staged copy
-      for (int p = w; p < NP; p += kWarps) {
-        const int o = s.poff[p], n = s.poff[p + 1] - o;
-        f3 q = mk(0.f, 0.f, 0.f);
-        if (lane < n) {
-          const int k = s.pvert[o + lane];
-          q = mk(a.xin[bj + k] + shift.x, a.yin[bj + k] + shift.y, a.zin[bj + k] + shift.z);
-        }
-        const float inv = 1.0f / (float)n;
-        const f3 cp = mk(warp_sum(q.x) * inv, warp_sum(q.y) * inv, warp_sum(q.z) * inv);
-        const f3 d = q - cp;
-        const float rad = warp_max(lane < n ? sqrtf(dot(d, d)) : 0.0f);
-        if (lane == 0) s.pb[p] = make_float4(cp.x, cp.y, cp.z, rad * (1.0f + 1e-6f));
-      }
+      stage_neighbour(s, a, j, shift, NV, NP, tid, w, lane);
       __syncthreads();
       const int ncand = *cnt;
       if (tid == 0) s.ncand[par ^ 1] = 0;
@@ -796,6 +838,75 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
     }
     // the last deferred sum's force lands after the loop's last barrier
     __syncthreads();
+  }
+
+  // AllVertAttraction (Cell3D_Kernel.cl:313-364), opt-in (Kat != 0): after
+  // the repulsion, every vertex gathers its pairs with the vertices of the
+  // cells on the list, neighbour by neighbour and patch by patch.  Pairs are
+  // skipped only where the reference's own test must fail: beyond
+  // 2 max(l0_i, l0_j) (with margins for the rounding of the periodic shift),
+  // judged in the frame of the centres' nearest image when every vertex pair
+  // of the two cells lies within L/2 of it on each axis (so the reference's
+  // per-pair wrap picks that same image); otherwise every pair is evaluated.
+  if (T.Kat != 0.0f) {
+    const int nnc = a.nn[c];
+    const bool scan_all =
+        nnc == kNbOverflow || *((volatile const int *)(a.stale + P.tissue)) != 0;
+    const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
+    const int *list = a.nbr + (size_t)c * kMaxNB3D;
+    const float L = T.L;
+    const float L0i = fmaxf(P.l0, 1e-12f);
+    for (int q = 0; q < count; ++q) {
+      const int j = scan_all ? T.cell_begin + q : list[q];
+      if (j == c) continue;
+      const Geom3D gj = a.geom_in[j];
+      const f3 shift = image_shift(gi, gj, T);
+      const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
+      const f3 dc = C - cj;
+      const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
+                        fabsf(C.z);
+      const float L0j = fmaxf(a.cells[j].l0, 1e-12f);
+      const float range = 2.0f * fmaxf(L0i, L0j) * (1.0f + 1e-4f) + 1e-5f * mag;
+      const float rr = (gi.R + gj.R) * (1.0f + 1e-4f) + range;
+      if (!(dot(dc, dc) <= rr * rr)) continue;
+      const float ext = gi.R + gj.R + range;
+      const bool prune = !T.pbc || (fabsf(dc.x) + ext < 0.49f * L &&
+                                    fabsf(dc.y) + ext < 0.49f * L &&
+                                    fabsf(dc.z) + ext < 0.49f * L);
+      stage_neighbour(s, a, j, shift, NV, NP, tid, w, lane);
+      __syncthreads();
+      const size_t bj = (size_t)j * NV;
+      const float range2 = range * range;
+      for (int v = tid; v < NV; v += kThreads) {
+        const f3 p = vtx(s, v);
+        const f3 d0 = p - cj;
+        const float rj = gj.R * (1.0f + 1e-4f) + range;
+        if (prune && !(dot(d0, d0) <= rj * rj)) continue;
+        float fx = s.fx[v], fy = s.fy[v], fz = s.fz[v];
+        for (int pp = 0; pp < NP; ++pp) {
+          if (prune) {
+            const float4 b = s.pb[pp];
+            const f3 d = p - mk(b.x, b.y, b.z);
+            const float rp = b.w + range;
+            if (!(dot(d, d) <= rp * rp)) continue;
+          }
+          const int o = s.poff[pp], n = s.poff[pp + 1] - o;
+          for (int i = 0; i < n; ++i) {
+            const int k = s.pvert[o + i];
+            if (prune) {
+              const f3 d = nbv(s, k) - p;
+              if (!(dot(d, d) <= range2)) continue;
+            }
+            const f3 qr = mk(a.xin[bj + k], a.yin[bj + k], a.zin[bj + k]);
+            attract_pair(p, qr, L0i, L0j, T.Kat, L, T.pbc != 0, fx, fy, fz);
+          }
+        }
+        s.fx[v] = fx;
+        s.fy[v] = fy;
+        s.fz[v] = fz;
+      }
+      __syncthreads();
+    }
   }
 
   // EulerPosition (Cell3D_Kernel.cl:371-381) and outputs
@@ -945,8 +1056,10 @@ __global__ void __launch_bounds__(256) k3d_binprep(Rebuild3DArgs a, int local_bi
   const int t = blockIdx.x;
   const Tissue3D T = a.tissues[t];
   float dmax = 0.0f;
-  for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x)
-    dmax = fmaxf(dmax, 2.0f * winding_reach(a.geom[c]));
+  for (int c = T.cell_begin + threadIdx.x; c < T.cell_end; c += blockDim.x) {
+    const Geom3D g = a.geom[c];
+    dmax = fmaxf(dmax, fmaxf(2.0f * winding_reach(g), 2.0f * g.R + T.arange));
+  }
   dmax = warp_max(dmax);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmax;
@@ -1003,9 +1116,11 @@ __device__ __forceinline__ bool pair3(const Geom3D &gi, const Geom3D &gj, const 
   }
   const float mag = __fadd_rn(__fadd_rn(__fadd_rn(fabsf(gi.cx), fabsf(gi.cy)), fabsf(gi.cz)), T.L);
   // vertices of i (within R_i) that can reach j (within its winding reach),
-  // or the other way round
+  // or the other way round; with the attraction, vertex pairs within its
+  // range
   const float ri = winding_reach(gi), rj = winding_reach(gj);
-  const float span = fmaxf(__fadd_rn(gi.R, rj), __fadd_rn(gj.R, ri));
+  const float span = fmaxf(fmaxf(__fadd_rn(gi.R, rj), __fadd_rn(gj.R, ri)),
+                           __fadd_rn(__fadd_rn(gi.R, gj.R), T.arange));
   const float m = __fadd_rn(__fmul_rn(1e-3f, span), __fmul_rn(1e-4f, mag));
   const float r = __fadd_rn(__fadd_rn(span, T.skin), m);
   const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));

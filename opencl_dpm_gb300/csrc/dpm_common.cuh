@@ -88,6 +88,10 @@ struct alignas(16) Tissue3D {
   float L, Kre, skin, binw;
   int pbc, cell_begin, cell_end, cap; // active cells [begin, end)
   int nb, cell_cap, steps_left, run_now;
+  // AllVertAttraction (opt-in; the reference's step loop never runs it):
+  // strength, and the pair range it needs (2 * largest l0, 0 when off)
+  float Kat, arange;
+  int pad0, pad1;
 };
 // Centre of mass, largest vertex distance from it, and the longest mesh
 // edge (the reference's winding sum drops faces whose denominator is below

@@ -138,14 +138,20 @@ struct dpm3d_batch {
     }
   }
 
-  // skin = skin_rel * mean cell diameter of each tissue
+  // skin = skin_rel * mean cell diameter of each tissue; the attraction's
+  // pair range, 2 * largest l0 (at least 1e-12) when Kat != 0
   void update_skin() {
     for (int t = 0; t < ntissues; ++t) {
       Tissue3D &T = h_tissues[t];
       double vs = 0.0;
-      for (int c = T.cell_begin; c < T.cell_end; ++c) vs += std::cbrt(h_cells[c].v0);
+      float l0max = 1e-12f;
+      for (int c = T.cell_begin; c < T.cell_end; ++c) {
+        vs += std::cbrt(h_cells[c].v0);
+        l0max = std::max(l0max, h_cells[c].l0);
+      }
       T.skin = (float)(skin_rel * 2.0 * std::cbrt(3.0 / (4.0 * M_PI)) * vs /
                        (T.cell_end - T.cell_begin));
+      T.arange = T.Kat != 0.0f ? 2.0f * l0max * (1.0f + 1e-4f) : 0.0f;
     }
   }
 
@@ -512,6 +518,24 @@ int dpm3d_set_tissues(dpm3d_batch *b, const float *L, const float *Kre, const in
   return DPM_OK;
 }
 
+int dpm3d_set_attraction(dpm3d_batch *b, const float *Kat) {
+  if (int r = check3(b)) return r;
+  if (!Kat) return fail(DPM_EINVAL, "null parameter array");
+  if (!b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues before the attraction");
+  for (int t = 0; t < b->ntissues; ++t) {
+    if (!std::isfinite(Kat[t])) return fail(DPM_EINVAL, "Kat must be finite");
+    b->h_tissues[t].Kat = Kat[t];
+  }
+  b->update_skin();
+  cudaSetDevice(b->ctx->device);
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue3D) * b->ntissues,
+                               cudaMemcpyHostToDevice, b->stream));
+  DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->clear_graphs();
+  return DPM_OK;
+}
+
 int dpm3d_upload(dpm3d_batch *b, const float *xyz) {
   if (int r = check3(b)) return r;
   if (!xyz) return fail(DPM_EINVAL, "null positions");
@@ -635,6 +659,8 @@ int dpm3d_save(dpm3d_batch *b, const char *path) {
   for (int t = 0; t < T; ++t) f.put1(b->h_tissues[t].pbc);
   f.put(xyz.data(), xyz.size());
   f.put(F.data(), F.size());
+  // trailing section: the attraction strength per tissue
+  for (int t = 0; t < T; ++t) f.put1(b->h_tissues[t].Kat);
   if (!f.ok() || f.close() != 0) return fail(DPM_EINVAL, std::string("write failed: ") + path);
   return DPM_OK;
 }
@@ -665,6 +691,8 @@ int dpm3d_open(dpm_ctx *ctx, const char *path, dpm3d_batch **out) {
     f.get(xyz.data(), xyz.size());
     f.get(F.data(), F.size());
     if (!f.ok()) return fail(DPM_EINVAL, "truncated checkpoint");
+    std::vector<float> Kat(T, 0.0f);
+    const bool att = f.try_get(Kat.data(), T);  // absent in older files
     long sum_nc = 0;
     for (int c : nc) sum_nc += c;
     if (sum_nc != N) return fail(DPM_EINVAL, "inconsistent checkpoint sizes");
@@ -673,6 +701,7 @@ int dpm3d_open(dpm_ctx *ctx, const char *path, dpm3d_batch **out) {
     int r = dpm3d_set_cells(b, k[0].data(), k[1].data(), k[2].data(), k[3].data(), k[4].data(),
                             k[5].data(), k[6].data(), k[7].data());
     if (!r) r = dpm3d_set_tissues(b, L.data(), Kre.data(), pbc.data());
+    if (!r && att) r = dpm3d_set_attraction(b, Kat.data());
     if (!r) r = dpm3d_upload(b, xyz.data());
     if (!r) {
       cudaError_t e = cudaSuccess;

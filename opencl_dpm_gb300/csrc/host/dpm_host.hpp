@@ -124,6 +124,9 @@ public:
   float L;
   float Kre = 0.0f;
   float Kat = 0.0f;
+  // extension: also run the reference's AllVertAttraction kernel with Kat
+  // (its own step loop never enqueues it, so Kat alone has no effect)
+  bool AllVertAttraction = false;
   std::string attractionMethod;
   std::vector<Cell3D> Cells;
   Tissue3D(std::vector<Cell3D> cells, float phi0);

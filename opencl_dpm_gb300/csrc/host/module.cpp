@@ -84,6 +84,9 @@ PYBIND11_MODULE(clDPM, m) {
       .def(py::init<std::vector<DPM::Cell3D>, float>(), py::arg("cells"), py::arg("phi0"))
       .def_readwrite("Kre", &DPM::Tissue3D::Kre)
       .def_readwrite("Kat", &DPM::Tissue3D::Kat)
+      .def_readwrite("AllVertAttraction", &DPM::Tissue3D::AllVertAttraction,
+                     "extension: run the reference's AllVertAttraction kernel with Kat "
+                     "after the repulsion (its own step loop never does)")
       .def_readwrite("Cells", &DPM::Tissue3D::Cells)
       .def_readonly("NCELLS", &DPM::Tissue3D::NCELLS)
       .def_readonly("L", &DPM::Tissue3D::L)

@@ -308,7 +308,8 @@ Tissue3D::Tissue3D(std::vector<Cell3D> cells, float phi0) {
 Tissue3D::~Tissue3D() { release(); }
 Tissue3D::Tissue3D(const Tissue3D &o)
     : NCELLS(o.NCELLS), PBC(o.PBC), L(o.L), Kre(o.Kre), Kat(o.Kat),
-      attractionMethod(o.attractionMethod), Cells(o.Cells) {}
+      AllVertAttraction(o.AllVertAttraction), attractionMethod(o.attractionMethod),
+      Cells(o.Cells) {}
 Tissue3D &Tissue3D::operator=(const Tissue3D &o) {
   if (this != &o) {
     release();
@@ -317,6 +318,7 @@ Tissue3D &Tissue3D::operator=(const Tissue3D &o) {
     L = o.L;
     Kre = o.Kre;
     Kat = o.Kat;
+    AllVertAttraction = o.AllVertAttraction;
     attractionMethod = o.attractionMethod;
     Cells = o.Cells;
   }
@@ -423,6 +425,8 @@ void Tissue3D::CLEulerUpdate(int nsteps, float dt) {
                         l0.data(), any_kb ? Kb.data() : nullptr, any_adh ? adh.data() : nullptr),
         "dpm3d_set_cells");
   check(dpm3d_set_tissues(batch_, &L, &Kre, &PBC), "dpm3d_set_tissues");
+  const float kat = AllVertAttraction ? Kat : 0.0f;
+  check(dpm3d_set_attraction(batch_, &kat), "dpm3d_set_attraction");
   check(dpm3d_upload(batch_, xyz.data()), "dpm3d_upload");
   check(dpm3d_step(batch_, nsteps, dt), "dpm3d_step");
   const int rc = dpm3d_download(batch_, xyz.data(), F.data());

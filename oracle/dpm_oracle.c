@@ -688,6 +688,59 @@ static void forces3d(const orc_tissue3d *t, const float *xyz, float *F,
     memset(wnflags, 0, (size_t)n * NV);
   }
   free(com);
+  /* AllVertAttraction, after the repulsion, when switched on */
+  if (t->Kat != 0.0f) orc_attraction3d(n, NV, xyz, t->l0, t->L, t->pbc, t->Kat, F);
+}
+
+/* AllVertAttraction (Cell3D_Kernel.cl:313-364).  The reference visits every
+ * ordered pair (vertex p1 of cell ci, vertex p2 of cell cj != ci): delta =
+ * p2 - p1, wrapped per axis by L*round(delta/L); dist = |delta|; with L0 =
+ * l0[ci] (at least 1e-12), if 1e-12 < dist < 2 L0 then tmp = Kat * 0.5 *
+ * (dist/L0 - 1) * (delta/dist) is subtracted from p1 and added to p2.  The
+ * visit from cj sees exactly -delta and the same dist, so vertex p1 gathers
+ * -tmp(L0 = l0[ci]) and +tmp'(L0 = l0[cj]) with tmp' built on -delta. */
+void orc_attraction3d(int ncells, int nv, const float *xyz, const float *l0, float L,
+                      int pbc, float Kat, float *F) {
+  if (Kat == 0.0f) return;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long gv = 0; gv < (long)ncells * nv; gv++) {
+    const int ci = (int)(gv / nv);
+    const float p1x = xyz[3 * gv], p1y = xyz[3 * gv + 1], p1z = xyz[3 * gv + 2];
+    float L0i = l0[ci];
+    if (L0i < 1e-12f) L0i = 1e-12f;
+    float fx = F[3 * gv], fy = F[3 * gv + 1], fz = F[3 * gv + 2];
+    for (int cj = 0; cj < ncells; cj++) {
+      if (cj == ci) continue;
+      float L0j = l0[cj];
+      if (L0j < 1e-12f) L0j = 1e-12f;
+      for (int vj = 0; vj < nv; vj++) {
+        const size_t k = (size_t)cj * nv + vj;
+        float dx = xyz[3 * k] - p1x, dy = xyz[3 * k + 1] - p1y, dz = xyz[3 * k + 2] - p1z;
+        if (pbc) {
+          const float rx = roundf(dx / L), ry = roundf(dy / L), rz = roundf(dz / L);
+          dx = dx - L * rx;
+          dy = dy - L * ry;
+          dz = dz - L * rz;
+        }
+        const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (dist < L0i * 2.0f && dist > 1e-12f) {
+          const float a = Kat * 0.5f * (dist / L0i - 1.0f);
+          fx = fx + -(a * (dx / dist));
+          fy = fy + -(a * (dy / dist));
+          fz = fz + -(a * (dz / dist));
+        }
+        if (dist < L0j * 2.0f && dist > 1e-12f) {
+          const float b = Kat * 0.5f * (dist / L0j - 1.0f);
+          fx = fx + b * (-dx / dist);
+          fy = fy + b * (-dy / dist);
+          fz = fz + b * (-dz / dist);
+        }
+      }
+    }
+    F[3 * gv] = fx;
+    F[3 * gv + 1] = fy;
+    F[3 * gv + 2] = fz;
+  }
 }
 
 /* Tissue3D::CLEulerUpdate (src/Tissue3D.cpp:372-445): per step clear,

@@ -63,6 +63,8 @@ typedef struct {
   const float *adh; /* [ncells] adhesion range (extension), or NULL = 2*l0 */
   int pbc;
   float L, Kre;
+  float Kat; /* AllVertAttraction strength; 0 = off (the reference's host loop
+              * never enqueues that kernel) */
 } orc_tissue3d;
 
 /* Runs nsteps in place on xyz; F receives the last step's forces (the
@@ -71,6 +73,12 @@ typedef struct {
  * number passed the threshold for each vertex in the last step. */
 int orc_run3d(const orc_tissue3d *t, float dt, int nsteps, float *xyz, float *F,
               unsigned char *wn, int nthreads);
+
+/* AllVertAttraction (shaders/Cell3D_Kernel.cl:313-364) on xyz ([ncells*nv]
+ * vertices), added into F, each vertex gathering its pairs over the other
+ * cells in ascending cell and vertex order. */
+void orc_attraction3d(int ncells, int nv, const float *xyz, const float *l0, float L,
+                      int pbc, float Kat, float *F);
 
 /* ---- initial dispersion (src/Tissue2D.cpp:42-114, src/Tissue3D.cpp:40-116) ---- */
 void orc_disperse2d(int ncells, const unsigned *nv, const unsigned *off,

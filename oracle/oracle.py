@@ -67,7 +67,8 @@ class _Tissue3D(ctypes.Structure):
     _fields_ = [("ncells", ctypes.c_int), ("nv", ctypes.c_int), ("nf", ctypes.c_int),
                 ("faces", _u32p), ("Kv", _f32p), ("Ka", _f32p), ("Ks", _f32p), ("v0", _f32p),
                 ("a0", _f32p), ("l0", _f32p), ("Kb", _f32p), ("adh", _f32p),
-                ("pbc", ctypes.c_int), ("L", ctypes.c_float), ("Kre", ctypes.c_float)]
+                ("pbc", ctypes.c_int), ("L", ctypes.c_float), ("Kre", ctypes.c_float),
+                ("Kat", ctypes.c_float)]
 
 
 @dataclass
@@ -114,6 +115,7 @@ class Tissue3DState:
     pbc: int = 1
     Kb: np.ndarray | None = None
     adh: np.ndarray | None = None
+    Kat: float = 0.0  # AllVertAttraction (off in the reference's own step loop)
 
     @property
     def ncells(self) -> int:
@@ -155,6 +157,8 @@ class Port:
         L.orc_diag2d.argtypes = [ctypes.POINTER(_Tissue2D), _f32p, _f64p, _f64p, _f64p]
         L.orc_diag3d.argtypes = [ctypes.POINTER(_Tissue3D), _f32p, _f64p, _f64p, _f64p]
         L.orc_bend_energy3d.argtypes = [ctypes.c_int, ctypes.c_int, _u32p, ctypes.c_double, _f64p]
+        L.orc_attraction3d.argtypes = [ctypes.c_int, ctypes.c_int, _f32p, _f32p, ctypes.c_float,
+                                       ctypes.c_int, ctypes.c_float, _f32p]
 
     # -- geometry --
     def cell2d(self, x0, y0, calA, nv, r0):
@@ -235,7 +239,7 @@ class Port:
         return _Tissue3D(s.ncells, s.nv, len(s.faces), _p(arrs["faces"], _u32p), _p(arrs["Kv"]),
                          _p(arrs["Ka"]), _p(arrs["Ks"]), _p(arrs["v0"]), _p(arrs["a0"]),
                          _p(arrs["l0"]), _p(arrs["Kb"]), _p(arrs["adh"]), int(s.pbc),
-                         float(s.L), float(s.Kre))
+                         float(s.L), float(s.Kre), float(s.Kat))
 
     def run3d(self, s: Tissue3DState, nsteps: int, dt: float, nthreads: int = 0):
         keep = []
@@ -248,6 +252,15 @@ class Port:
         if rc:
             raise RuntimeError(f"orc_run3d failed ({rc})")
         return F, flags
+
+    def attraction3d(self, xyz, nv, l0, L, pbc, Kat):
+        """AllVertAttraction alone: the forces it adds, [ncells*nv, 3]."""
+        xyz = _f32(xyz)
+        l0 = _f32(l0)
+        F = np.zeros_like(xyz)
+        self.lib.orc_attraction3d(len(l0), nv, _p(xyz), _p(l0), float(L), int(pbc), float(Kat),
+                                  _p(F))
+        return F
 
     def disperse2d(self, nv, r0, L, seed):
         nv = _u32(nv)
@@ -310,6 +323,9 @@ class Ref:
                                        _f32p, _f32p]
         self.lib.ref3d_cell.argtypes = [_f32p, ctypes.c_float, ctypes.c_float, _f32p, _u32p,
                                         _f32p, _f32p, _f32p, _f32p, _f32p]
+        self.lib.ref3d_attraction.argtypes = [ctypes.c_char_p, ctypes.c_int, _f32p, _f32p,
+                                              ctypes.c_float, ctypes.c_int, ctypes.c_float,
+                                              _f32p]
         self.lib.ref3d_run.argtypes = [ctypes.c_char_p, ctypes.c_int, _f32p, _f32p, _f32p,
                                        _f32p, _f32p, _f32p, _f32p, ctypes.c_float,
                                        ctypes.c_float, ctypes.c_int, ctypes.c_long,
@@ -370,3 +386,15 @@ class Ref:
         if rc:
             raise RuntimeError(f"ref3d_run: {self.lib.ref_last_error().decode()}")
         return xo, fo, vo, so, Lo.value
+
+    def attraction3d(self, xyz, l0, L, pbc, Kat):
+        """The reference's AllVertAttraction kernel run once through its own
+        OpenCL calls on the CPU shim (162 vertices per cell)."""
+        xyz = _f32(xyz)
+        l0 = _f32(l0)
+        F = np.zeros_like(xyz)
+        rc = self.lib.ref3d_attraction(self.refdir, len(l0), _p(xyz), _p(l0), float(L), int(pbc),
+                                       float(Kat), _p(F))
+        if rc:
+            raise RuntimeError(f"ref3d_attraction: {self.lib.ref_last_error().decode()}")
+        return F

@@ -12,6 +12,7 @@
 // call.
 #include "Tissue.hpp"
 #include "cell.hpp"
+#include "readKernel.hpp"
 
 #include <cstdio>
 #include <cstdlib>
@@ -202,6 +203,72 @@ int ref3d_run(const char *refdir, int ncells, const float *start,
       sa_out[ci] = T.Cells[ci].GetSurfaceArea();
     }
     *L_out = T.L;
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return 2;
+  }
+}
+
+// Runs the reference's AllVertAttraction kernel (shaders/Cell3D_Kernel.cl:
+// 313-364), which its own step loop never enqueues, once on the given
+// vertices (162 per cell), with the OpenCL calls its host code makes for the
+// other 3D kernels (src/Tissue3D.cpp:199-426): build, buffers, setArg,
+// NDRange(NV, NCELLS), read back.  forces_out receives the forces, which
+// start from zero.
+int ref3d_attraction(const char *refdir, int ncells, const float *xyz, const float *l0,
+                     float L, int pbc, float Kat, float *forces_out) {
+  try {
+    CwdGuard cwd(refdir);
+    if (!cwd.ok) {
+      g_last_error = "cannot enter reference directory";
+      return 1;
+    }
+    const unsigned NV = DPM::Cell3D::NV;
+    const size_t n = (size_t)ncells * NV;
+    cl::Device device = cl::Device::getDefault();
+    cl::Context context({device});
+    cl::Program program(context, readKernelSource("shaders/Cell3D_Kernel.cl"));
+    if (program.build({device}, "-cl-opt-disable -Werror") != CL_SUCCESS) {
+      g_last_error = "kernel build failed";
+      return 2;
+    }
+    std::vector<cl_float3> verts(n), forces(n);
+    for (size_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) {
+        verts[i].s[k] = xyz[3 * i + k];
+        forces[i].s[k] = 0.0f;
+      }
+    std::vector<float> l0v(l0, l0 + ncells);
+    cl::Buffer gpuVerts(context, CL_MEM_READ_ONLY | CL_MEM_COPY_HOST_PTR,
+                        sizeof(cl_float3) * n, verts.data());
+    cl::Buffer gpuForces(context, CL_MEM_READ_WRITE | CL_MEM_COPY_HOST_PTR,
+                         sizeof(cl_float3) * n, forces.data());
+    cl::Buffer gpul0(context, CL_MEM_READ_ONLY | CL_MEM_COPY_HOST_PTR,
+                     sizeof(float) * ncells, l0v.data());
+    cl_int err = CL_SUCCESS;
+    cl::Kernel kernel(program, "AllVertAttraction", &err);
+    if (err != CL_SUCCESS) {
+      g_last_error = "no AllVertAttraction kernel";
+      return 3;
+    }
+    kernel.setArg(0, gpuVerts);
+    kernel.setArg(1, gpuForces);
+    kernel.setArg(2, gpul0);
+    kernel.setArg(3, L);
+    kernel.setArg(4, ncells);
+    kernel.setArg(5, pbc);
+    kernel.setArg(6, Kat);
+    cl::CommandQueue queue(context, device, 0, &err);
+    err = queue.enqueueNDRangeKernel(kernel, cl::NullRange, cl::NDRange(NV, ncells));
+    if (err == CL_SUCCESS)
+      err = queue.enqueueReadBuffer(gpuForces, CL_TRUE, 0, sizeof(cl_float3) * n, forces.data());
+    if (err != CL_SUCCESS) {
+      g_last_error = "AllVertAttraction launch failed";
+      return 4;
+    }
+    for (size_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) forces_out[3 * i + k] = forces[i].s[k];
     return 0;
   } catch (const std::exception &e) {
     g_last_error = e.what();

@@ -107,6 +107,8 @@ def gpu_batch3d(ctx, states, tuning=None):
         adh = np.concatenate([s.adh if s.adh is not None else 2.0 * s.l0 for s in states])
     b.set_cells(cat("Kv"), cat("Ka"), cat("Ks"), cat("v0"), cat("a0"), cat("l0"), kb, adh)
     b.set_tissues([s.L for s in states], [s.Kre for s in states], [s.pbc for s in states])
+    if any(s.Kat != 0.0 for s in states):
+        b.set_attraction([s.Kat for s in states])
     if tuning:
         b.set_tuning(**tuning)
     b.upload(np.concatenate([s.xyz for s in states]))

@@ -108,7 +108,24 @@ def main():
                               nsteps=0)
     np.savez_compressed(os.path.join(HERE, "disperse_3d.npz"), xyz=x6, L=np.float32(L6),
                         seed=np.int64(3), phi0=np.float32(0.35))
+    attraction_case(R, out)
     print("golden vectors written to", HERE)
+
+
+def attraction_case(R, run3d_out):
+    """The reference's AllVertAttraction kernel (never enqueued by its step
+    loop) on the 20-step state of run_3d, cells in contact, with the rest
+    edge of the reference's 3D tissue as l0."""
+    from oracle.oracle import Port
+    xyz = run3d_out["xyz_20"]
+    n = len(run3d_out["start"])
+    _, _, _, _, a0, _, _ = R.cell3d([0.0, 0.0, 0.0], 1.05, 1.0)
+    l0 = np.full(n, Port().l0_3d(a0), np.float32)
+    L = np.float32(run3d_out["L"])
+    Kat = np.float32(0.3)
+    F = R.attraction3d(xyz, l0, L, 1, Kat)
+    np.savez_compressed(os.path.join(HERE, "attraction_3d.npz"), xyz=xyz, l0=l0, L=L, Kat=Kat,
+                        pbc=np.int32(1), F=F)
 
 
 if __name__ == "__main__":

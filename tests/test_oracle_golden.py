@@ -154,3 +154,29 @@ def test_port_matches_reference_live(seed):
     s = state2d_from_golden(g)
     F, _ = port().run2d(s, 30, 0.005)
     assert np.array_equal(s.xy, xo) and np.array_equal(F, fo)
+
+
+def test_attraction_3d_golden():
+    """AllVertAttraction (never enqueued by the reference's step loop): the
+    oracle gathers each vertex's pairs in cell and vertex order, the
+    reference scatters them with float atomics, so the sums agree to
+    rounding (relative 1e-6), term by term the same arithmetic."""
+    g = load("attraction_3d")
+    F = port().attraction3d(g["xyz"], 162, g["l0"], float(g["L"]), int(g["pbc"]),
+                            float(g["Kat"]))
+    ref = g["F"]
+    assert np.count_nonzero(np.abs(ref).sum(1)) > 100
+    assert np.array_equal(np.abs(F).sum(1) == 0, np.abs(ref).sum(1) == 0)
+    assert np.linalg.norm(F - ref) <= 1e-6 * np.linalg.norm(ref)
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("pbc", [0, 1])
+def test_attraction_3d_live(pbc):
+    from cases import make_tissue3d
+    s = make_tissue3d(6, level=2, phi0=0.5, seed=3)
+    l0 = s.l0 * np.float32(1.5)  # a longer range: more pairs
+    ref = Ref().attraction3d(s.xyz, l0, s.L, pbc, 0.7)
+    F = port().attraction3d(s.xyz, s.nv, l0, s.L, pbc, 0.7)
+    assert np.count_nonzero(np.abs(ref).sum(1)) > 100
+    assert np.linalg.norm(F - ref) <= 1e-6 * np.linalg.norm(ref)
