@@ -60,9 +60,18 @@ cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_
 cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
 // One fused time step.  warps: 4, 8 or 16 per block; variant bit 0 caps
 // registers for 32 resident warps per SM (else the compiler chooses), bit 1
-// selects the dynamic schedule (needs a.sched).
+// selects the dynamic schedule (needs a.sched), bit 2 compiles the
+// attraction in (needed when any tissue has Kat != 0; without it the kernel
+// is smaller and faster).
 cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int variant,
                           cudaStream_t s);
+// The same for 32*S vertex slots per warp (dpm2d_step_s<S>.cu).
+cudaError_t launch_step2d_s1(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
+cudaError_t launch_step2d_s2(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
+cudaError_t launch_step2d_s4(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
+cudaError_t launch_step2d_s8(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
+cudaError_t launch_step2d_s8_att(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
+constexpr int kStepVariantAttraction = 4;
 
 // Host mirror of the bin arithmetic (for the host rebuild check).
 int bin_axis_count(float L, float w, int cap);

@@ -229,7 +229,7 @@ extern "C" int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *K
       a.dt = dt;
       a.step_index = i;
       a.all_forces = 1;
-      DPM_CUDA_TRY(launch_step2d(a, maxnv, 8, 1, s));
+      DPM_CUDA_TRY(launch_step2d(a, maxnv, 8, Kat != 0.0f ? 1 | kStepVariantAttraction : 1, s));
       cur = 1 - cur;
     }
     done += len;

@@ -101,6 +101,7 @@ struct dpm2d_batch {
   float skin_rel = 0.15f;
   int warps = 8;
   int occ = 1;
+  bool att = false;     // some tissue has Kat != 0: launch the step with attraction
   bool serving = false; // slot pool of a server: per-tissue step budgets
   long rebuilds = 0;
 
@@ -123,6 +124,9 @@ struct dpm2d_batch {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
   }
+  // the step kernel's variant: the tuned occupancy/schedule bits, and the
+  // attraction compiled in only when a tissue uses it
+  int variant() const { return occ | (att ? kStepVariantAttraction : 0); }
 
   Rebuild2DArgs rebuild_args() const {
     Rebuild2DArgs a{};
@@ -196,7 +200,7 @@ struct dpm2d_batch {
     if (e != cudaSuccess) return e;
     int f = from;
     for (int i = 0; i < len; ++i) {
-      e = launch_step2d(step_args(f, dt, last && i == len - 1, i), maxnv, warps, occ, s);
+      e = launch_step2d(step_args(f, dt, last && i == len - 1, i), maxnv, warps, variant(), s);
       if (e != cudaSuccess) return e;
       f = 1 - f;
     }
@@ -452,6 +456,7 @@ int dpm2d_set_tissues(dpm2d_batch *b, const float *L, const float *Kre, const fl
   if (int r = check_batch(b)) return r;
   if (!L || !Kre || !Kat || !pbc) return fail(DPM_EINVAL, "null parameter array");
   int max_local = 1;
+  bool att = false;
   for (int t = 0; t < b->ntissues; ++t) {
     if (!(L[t] > 0.0f) || !std::isfinite(L[t])) return fail(DPM_EINVAL, "L must be positive");
     Tissue2D &T = b->h_tissues[t];
@@ -459,6 +464,7 @@ int dpm2d_set_tissues(dpm2d_batch *b, const float *L, const float *Kre, const fl
     T.Kre = Kre[t];
     T.Kat = Kat[t];
     T.pbc = pbc[t] ? 1 : 0;
+    att |= Kat[t] != 0.0f;
     // bins per axis never need to be narrower than a cell radius
     float a0max = 0.0f;
     for (int c = T.cell_begin; c < T.cell_end; ++c) a0max = std::max(a0max, b->h_cells[c].a0);
@@ -471,6 +477,7 @@ int dpm2d_set_tissues(dpm2d_batch *b, const float *L, const float *Kre, const fl
   b->local_bits = std::max(1, max_local);
   b->key_bits = b->local_bits + ceil_log2(b->ntissues);
   if (b->key_bits > 32) return fail(DPM_ECAPACITY, "cell-list keys exceed 32 bits");
+  b->att = att;
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue2D) * b->ntissues,
                                cudaMemcpyHostToDevice, b->stream));
@@ -541,7 +548,7 @@ int dpm2d_step_kernel(dpm2d_batch *b, float dt) {
   if (int r = check_batch(b)) return r;
   if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before stepping");
   cudaSetDevice(b->ctx->device);
-  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true, 0), b->maxnv, b->warps, b->occ,
+  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true, 0), b->maxnv, b->warps, b->variant(),
                              b->stream));
   b->cur = 1 - b->cur;
   return DPM_OK;
@@ -1089,6 +1096,11 @@ int pool2d_assign(dpm2d_batch *b, int slot, int ncells, const unsigned *nv, cons
   T.Kat = Kat;
   T.pbc = pbc ? 1 : 0;
   T.l0max = l0max;
+  if (Kat != 0.0f && !b->att) {
+    // a slot pool keeps the attraction variant once a run has needed it
+    b->att = true;
+    b->clear_graphs();
+  }
   T.skin = (float)(b->skin_rel * 2.0 * rsum / ncells);
   const double rad = std::sqrt(a0max / M_PI);
   long cap = (long)std::floor(L / std::max(rad, 1e-6));

@@ -222,3 +222,25 @@ def test_kernel_variants_identical(ctx):
     ref = out[(1, 8)]
     for k, (xy, F) in out.items():
         assert np.array_equal(xy, ref[0]) and np.array_equal(F, ref[1]), k
+
+
+def test_attraction_variant_same_bits(ctx):
+    """A batch with one tissue using the attraction runs the step with the
+    attraction compiled in; its other tissues (Kat = 0) must come out with
+    the same bits as alone, where the smaller kernel without it runs."""
+    states = [make_tissue2d(24, 24, phi=0.8, seed=40 + t, Kb=0.01) for t in range(3)]
+    att = make_tissue2d(20, 32, phi=0.85, seed=50)
+    att.Kat = 0.3
+    b = gpu_batch2d(ctx, states + [att])
+    b.step(40, DT)
+    xy, _ = b.download()
+    off = 0
+    for s in states:
+        nvt = int(s.nv.sum())
+        a = gpu_batch2d(ctx, [s])
+        a.step(40, DT)
+        ax, _ = a.download()
+        assert np.array_equal(ax, xy[off:off + nvt])
+        off += nvt
+    rx, _, _ = oracle_run(att, 40)
+    assert pos_err(xy[off:], rx) <= X_TOL
