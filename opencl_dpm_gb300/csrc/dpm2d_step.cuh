@@ -113,12 +113,19 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     const int q = base + lane;
     int jl = -1;
     unsigned pflags = 0u;
+    unsigned jvoff = 0u, jnv = 0u;
     Geom2D gl;
     gl.cx = gl.cy = gl.R = gl.area = gl.minx = gl.maxx = gl.miny = gl.maxy = 0.0f;
     if (q < count) {
       jl = scan_all ? T.cell_begin + q : list[q];
       if (jl != c) {
+        // the ring's place (first vertex, count), loaded beside the
+        // geometry for all 32 entries at once rather than one round trip
+        // per passing cell below
+        const uint4 r = *reinterpret_cast<const uint4 *>(a.cells + jl);
         gl = a.geom_in[jl];
+        jvoff = r.x;
+        jnv = r.y;
         const float dcx = gi.cx - gl.cx, dcy = gi.cy - gl.cy;
         const float rr = gi.R + gl.R;
         const float mm = kRelMargin * rr + kAbsMargin * (fabsf(gi.cx) + fabsf(gi.cy) +
@@ -146,8 +153,8 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     while (pm) {
     const int src = __ffs(pm) - 1;
     pm &= pm - 1u;
-    const int j = __shfl_sync(kFull, jl, src);
     const unsigned fl = __shfl_sync(kFull, pflags, src);
+    const unsigned jx = __shfl_sync(kFull, jvoff, src), jy = __shfl_sync(kFull, jnv, src);
     const bool near = fl & 1u, far = fl & 2u, attp = fl & 4u;
     Geom2D gj;
     gj.cx = __shfl_sync(kFull, gl.cx, src);
@@ -192,9 +199,8 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
       }
     }
     if (!anyc && !anya && !anyx) continue;
-    const uint4 jr = *reinterpret_cast<const uint4 *>(a.cells + j);
-    const int nj = (int)jr.y;
-    const float2 *pj = a.pos_in + jr.x;
+    const int nj = (int)jy;
+    const float2 *pj = a.pos_in + jx;
     if (anyx) {
       // kCheckY points are candidates only if a ring vertex has y offset
       // exactly -L; kCheckX points only if one has x offset within 8 ulp(L)
