@@ -153,3 +153,19 @@ def test_3d_single_cell_and_far_neighbours(ctx):
     r = s.copy()
     port().run3d(r, 5, DT)
     assert pos_err(x.reshape(-1), r.xyz.reshape(-1)) <= X_TOL
+
+
+@pytest.mark.parametrize("nv", [100, 200])
+def test_large_rings_with_attraction(ctx, nv):
+    """Rings of more than 64 vertices (4 and 8 slots per lane) with the
+    attraction compiled in, against the oracle."""
+    s = make_tissue2d(6, nv, calA=1.1, Kb=0.01, phi=0.85, Kat=0.4, seed=nv)
+    for steps in (1, 20):
+        b = gpu_batch2d(ctx, [s])
+        b.step(steps, 0.001)
+        x, F = b.download()
+        r = s.copy()
+        rF, _ = port().run2d(r, steps, 0.001)
+        assert pos_err(x, r.xy) <= X_TOL
+        if steps == 1:
+            assert rel_norm_err(F, rF) <= F_TOL
