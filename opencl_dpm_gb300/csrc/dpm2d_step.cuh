@@ -15,10 +15,13 @@ namespace {
 // ---------------------------------------------------------------------------
 
 // Occupancy variants: with OCC = 1 the register budget is capped so that
-// 32 warps per SM stay resident (16 for more than 2 vertex slots per lane);
-// with OCC = 0 the compiler chooses.  The tuner picks per batch.
+// 48 warps per SM stay resident (40 registers, a few spilled: the step
+// waits mostly on L2 loads of the neighbours' rings, and more resident
+// warps hide them better than 32 warps at 64 registers; 16 warps for more
+// than 2 vertex slots per lane); with OCC = 0 the compiler chooses.  The
+// tuner picks per batch.
 template <int S, int W, int OCC> struct StepOcc {
-  static constexpr int kThreads = S <= 2 ? 1024 : 512;
+  static constexpr int kThreads = S <= 2 ? 1536 : 512;
   static constexpr int kBlocks =
       OCC == 0 ? 1 : (kThreads / (W * 32) > 0 ? kThreads / (W * 32) : 1);
 };
