@@ -270,24 +270,29 @@ __global__ void __launch_bounds__(kNbWarps * 32) k2d_neighbors(Rebuild2DArgs a, 
   const int nb = T.nbx;
   const float inv = __fdiv_rn((float)nb, T.L);
   const int bx = bin_of(gi.cx, T.L, inv, nb), by = bin_of(gi.cy, T.L, inv, nb);
-  // distinct bin offsets along an axis with nb bins
+  // distinct bin offsets along an axis with nb bins; lane l finds the
+  // sorted range of the l-th neighbouring bin (the searches run side by
+  // side), then the bins are visited in order
   const int lo_off = nb >= 3 ? -1 : 0, hi_off = nb >= 3 ? 1 : nb - 1;
-  for (int oy = lo_off; oy <= hi_off; ++oy) {
-    const int yy = (by + oy + nb) % nb;
-    for (int ox = lo_off; ox <= hi_off; ++ox) {
-      const int xx = (bx + ox + nb) % nb;
-      const uint32_t key = ((uint32_t)t << local_bits) | (uint32_t)(yy * nb + xx);
-      const int lo = lower_bound_u32(a.sorted_keys, T.cell_begin, T.cell_end, key);
-      const int hi = lower_bound_u32(a.sorted_keys, lo, T.cell_end, key + 1u);
-      for (int base = lo; base < hi; base += 32) {
-        const int q = base + lane;
-        const int j = q < hi ? (int)a.sorted_vals[q] : -1;
-        const bool ok = j >= 0 && j != c && pair_near(gi, a.geom[j], T, cp.l0);
-        const unsigned m = __ballot_sync(kFull, ok);
-        const int pos = cnt + __popc(m & lt);
-        if (ok && pos < kNbBuf) buf[w][pos] = j;
-        cnt += __popc(m);
-      }
+  const int nax = hi_off - lo_off + 1, nbins = nax * nax;
+  int blo = 0, bhi = 0;
+  if (lane < nbins) {
+    const int yy = (by + lo_off + lane / nax + nb) % nb;
+    const int xx = (bx + lo_off + lane % nax + nb) % nb;
+    const uint32_t key = ((uint32_t)t << local_bits) | (uint32_t)(yy * nb + xx);
+    blo = lower_bound_u32(a.sorted_keys, T.cell_begin, T.cell_end, key);
+    bhi = lower_bound_u32(a.sorted_keys, blo, T.cell_end, key + 1u);
+  }
+  for (int bin = 0; bin < nbins; ++bin) {
+    const int lo = __shfl_sync(kFull, blo, bin), hi = __shfl_sync(kFull, bhi, bin);
+    for (int base = lo; base < hi; base += 32) {
+      const int q = base + lane;
+      const int j = q < hi ? (int)a.sorted_vals[q] : -1;
+      const bool ok = j >= 0 && j != c && pair_near(gi, a.geom[j], T, cp.l0);
+      const unsigned m = __ballot_sync(kFull, ok);
+      const int pos = cnt + __popc(m & lt);
+      if (ok && pos < kNbBuf) buf[w][pos] = j;
+      cnt += __popc(m);
     }
   }
   // pairs whose raw offsets can exceed L (the reference's shifted edges)

@@ -1145,25 +1145,32 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
   const float inv = __fdiv_rn((float)nb, T.L);
   const int bx = bin3(gi.cx, T.L, inv, nb), by = bin3(gi.cy, T.L, inv, nb),
             bz = bin3(gi.cz, T.L, inv, nb);
+  // lane l finds the sorted range of the l-th neighbouring bin (the
+  // searches run side by side), then the bins are visited in order
   const int lo_off = nb >= 3 ? -1 : 0, hi_off = nb >= 3 ? 1 : nb - 1;
+  const int nax = hi_off - lo_off + 1, nbins = nax * nax * nax;  // at most 27
+  int blo = 0, bhi = 0;
+  if (lane < nbins) {
+    const int oz = lo_off + lane / (nax * nax), oy = lo_off + (lane / nax) % nax,
+              ox = lo_off + lane % nax;
+    const int xx = (bx + ox + nb) % nb, yy = (by + oy + nb) % nb, zz = (bz + oz + nb) % nb;
+    const uint32_t key = ((uint32_t)t << local_bits) | (uint32_t)((zz * nb + yy) * nb + xx);
+    blo = lb_u32(a.sorted_keys, T.cell_begin, T.cell_end, key);
+    bhi = lb_u32(a.sorted_keys, blo, T.cell_end, key + 1u);
+  }
   int cnt = 0;
-  for (int oz = lo_off; oz <= hi_off; ++oz)
-    for (int oy = lo_off; oy <= hi_off; ++oy)
-      for (int ox = lo_off; ox <= hi_off; ++ox) {
-        const int xx = (bx + ox + nb) % nb, yy = (by + oy + nb) % nb, zz = (bz + oz + nb) % nb;
-        const uint32_t key = ((uint32_t)t << local_bits) | (uint32_t)((zz * nb + yy) * nb + xx);
-        const int lo = lb_u32(a.sorted_keys, T.cell_begin, T.cell_end, key);
-        const int hi = lb_u32(a.sorted_keys, lo, T.cell_end, key + 1u);
-        for (int b0 = lo; b0 < hi; b0 += 32) {
-          const int q = b0 + lane;
-          const int j = q < hi ? (int)a.sorted_vals[q] : -1;
-          const bool ok = j >= 0 && j != c && pair3(gi, a.geom[j], T);
-          const unsigned m = __ballot_sync(kFull, ok);
-          const int pos = cnt + __popc(m & lt);
-          if (ok && pos < kNb3Buf) buf[w][pos] = j;
-          cnt += __popc(m);
-        }
-      }
+  for (int bin = 0; bin < nbins; ++bin) {
+    const int lo = __shfl_sync(kFull, blo, bin), hi = __shfl_sync(kFull, bhi, bin);
+    for (int b0 = lo; b0 < hi; b0 += 32) {
+      const int q = b0 + lane;
+      const int j = q < hi ? (int)a.sorted_vals[q] : -1;
+      const bool ok = j >= 0 && j != c && pair3(gi, a.geom[j], T);
+      const unsigned m = __ballot_sync(kFull, ok);
+      const int pos = cnt + __popc(m & lt);
+      if (ok && pos < kNb3Buf) buf[w][pos] = j;
+      cnt += __popc(m);
+    }
+  }
   __syncwarp();
   int nout;
   if (cnt > kNb3Buf) {
