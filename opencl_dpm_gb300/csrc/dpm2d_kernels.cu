@@ -1,20 +1,24 @@
-// 2D DPM kernels for sm_103a.
+// 2D DPM kernels for sm_103a: initial geometry, diagnostics, the cell list
+// (bin keys, neighbour lists) and the dispatch of the fused step.
 //
 // One warp owns one cell per launch.  A time step is ONE fused kernel
-// (k2d_step): it reads the cell's vertex ring once, computes the area,
-// perimeter and bending forces from the ring held in shared memory, the
-// attraction and repulsion against the cells of its neighbour list, applies
-// the overdamped Euler update, writes the new positions, and -- as its
-// epilogue -- the geometry of the new positions (centre, enclosing radius,
-// area, box) that the next step's neighbour tests read.  The force field is
-// never stored unless the caller asks for the last step's forces.
+// (k2d_step, in dpm2d_step.cuh): it reads the cell's vertex ring once,
+// computes the area, perimeter and bending forces from the ring held in
+// shared memory, the attraction and repulsion against the cells of its
+// neighbour list, applies the overdamped Euler update, writes the new
+// positions, and -- as its epilogue -- the geometry of the new positions
+// (centre, enclosing radius, area, box) that the next step's neighbour tests
+// read.  The force field is never stored unless the caller asks for the last
+// step's forces.
 //
 // Physics follows the reference kernels (shaders/Cell2D_kernel.cl); the
 // repulsion's containment test uses the reference's exact crossing
 // arithmetic (each operation rounded separately, no contraction), so that a
 // vertex is flagged inside another cell on exactly the same inputs as the
 // reference flags it.  Candidate cells are pruned with tests that are proved
-// conservative (see `vertex_candidate`), so pruning never changes a flag.
+// conservative (see `vertex_candidate` in dpm2d_device.cuh), so pruning
+// never changes a flag; the neighbour lists below only ever hold more cells
+// than those tests need.
 #include "dpm2d_kernels.cuh"
 
 #include <math.h>
