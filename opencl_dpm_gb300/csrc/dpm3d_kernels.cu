@@ -11,12 +11,17 @@
 //     deterministic (shaders/Cell3D_Kernel.cl:66-247);
 //   * optional triangle bending (extension);
 //   * repulsion by winding number against the cells of the neighbour list
-//     (Cell3D_Kernel.cl:251-310): candidate vertices inside the neighbour's
-//     bounding sphere are compacted, one warp evaluates one candidate's
-//     solid-angle sum over the neighbour's faces with the neighbour's
-//     vertices staged in shared memory;
+//     (Cell3D_Kernel.cl:251-310): the neighbour's vertices are staged in
+//     shared memory with the bounding spheres of their patches, candidate
+//     vertices within its winding reach are compacted, and one warp decides
+//     each candidate's winding number -- by a separating plane (outside) or
+//     the neighbour's inner ball (inside), adding only the terms of the faces
+//     the reference drops -- or defers it to a sum over every face that the
+//     whole block evaluates (winding_at);
+//   * opt-in AllVertAttraction (Cell3D_Kernel.cl:313-364);
 //   * Euler update x += F*dt (Cell3D_Kernel.cl:371-381) and, as epilogue, the
-//     centre and bounding radius of the new mesh for the next step.
+//     centre, bounding radius, longest edge and inner ball of the new mesh for
+//     the next step.
 #include "dpm3d_kernels.cuh"
 
 #include <math.h>
