@@ -123,3 +123,24 @@ def test_deterministic_3d(ctx):
         b.step(10, DT)
         out.append(b.download())
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_monolayer_level3_contacts(ctx):
+    """A contact-rich monolayer at subdivision 3 (642 vertices, jittered
+    hexagonal lattice, overlapping neighbours): the candidates go through
+    every winding certificate (centre-direction support, inner ball, face
+    plane) and the deferred full sums."""
+    import bench
+    from opencl_dpm_gb300 import clDPM
+    from oracle.oracle import Tissue3DState
+    t = bench.build_monolayer(clDPM, np.random.default_rng(11), 16, 3)
+    s = Tissue3DState(nv=t["nv"], faces=t["faces"], xyz=t["xyz"].copy(), Kv=t["Kv"], Ka=t["Ka"],
+                      Ks=t["Ks"], v0=t["v0"], a0=t["a0"], l0=t["l0"], L=float(t["L"]), Kre=1.0,
+                      pbc=1, Kb=t["Kb"], adh=t["adh"])
+    for nsteps in (1, 10):
+        x, F, wn, rx, rF, rwn = run_case(ctx, s, nsteps)
+        assert rwn.sum() > 100  # many vertices inside a neighbour
+        assert wn_mismatch(wn, rwn) <= 2e-3
+        assert pos_err(x, rx) <= X_TOL
+        if nsteps == 1:
+            assert rel_norm_err(F, rF) <= F_TOL
