@@ -26,6 +26,8 @@
 
 #include <math.h>
 
+#include <mutex>
+
 namespace dpm {
 
 namespace {
@@ -1220,9 +1222,21 @@ size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend) {
   return sizeof(float4) * kMaxPatches3D + floats * 4 + halves * 2 + (size_t)nv + 16;
 }
 
+// The kernel's dynamic shared-memory limit is a per-device attribute shared
+// by every batch: it is only ever raised, so a batch of a smaller mesh made
+// after a larger one does not lower it under the larger one's launches.
 cudaError_t prepare_step3d(int nv, int nf, int ne, bool bend) {
+  static std::mutex mu;
+  static size_t granted[64] = {0};
   const size_t bytes = step3d_smem_bytes(nv, nf, ne, bend);
-  return cudaFuncSetAttribute(k3d_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev >= 0 && dev < 64 && bytes <= granted[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(k3d_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess && dev >= 0 && dev < 64) granted[dev] = bytes;
+  return e;
 }
 
 cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {

@@ -144,3 +144,18 @@ def test_monolayer_level3_contacts(ctx):
         assert pos_err(x, rx) <= X_TOL
         if nsteps == 1:
             assert rel_norm_err(F, rF) <= F_TOL
+
+
+def test_larger_mesh_after_smaller(ctx):
+    """A batch of a larger mesh still steps after a batch of a smaller mesh
+    was made (the step's shared-memory limit is shared by all batches)."""
+    s3 = make_tissue3d(2, level=3, phi0=0.5, seed=5)
+    b3 = gpu_batch3d(ctx, [s3])
+    s2 = make_tissue3d(2, level=2, phi0=0.5, seed=5)
+    b2 = gpu_batch3d(ctx, [s2])
+    b3.step(2, DT)
+    b2.step(2, DT)
+    x3, _ = b3.download()
+    r = s3.copy()
+    port().run3d(r, 2, DT)
+    assert pos_err(x3, r.xyz) <= X_TOL
