@@ -418,20 +418,28 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
 template <int S, int W, int OCC, bool ATT>
 cudaError_t launch_step_sw(const Step2DArgs &a, bool dyn, cudaStream_t s) {
   if (dyn && a.sched) {
-    // resident blocks per SM of this variant, and the device's SM count
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0) {
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm, k2d_step_dyn<S, W, OCC, ATT>, W * 32, 0);
-      if (e != cudaSuccess) return e;
+    // resident blocks per SM of this variant and the device's SM count,
+    // found once (a function-local static: initialised once even when
+    // several host threads launch at the same time)
+    struct Resident {
+      int per_sm, sms;
+      cudaError_t err;
+    };
+    static const Resident res = [] {
+      Resident r{0, 0, cudaSuccess};
+      r.err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &r.per_sm, k2d_step_dyn<S, W, OCC, ATT>, W * 32, 0);
       int dev = 0;
-      e = cudaGetDevice(&dev);
-      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      if (e != cudaSuccess) return e;
-      if (per_sm < 1) per_sm = 1;
-    }
+      if (r.err == cudaSuccess) r.err = cudaGetDevice(&dev);
+      if (r.err == cudaSuccess)
+        r.err = cudaDeviceGetAttribute(&r.sms, cudaDevAttrMultiProcessorCount, dev);
+      if (r.per_sm < 1) r.per_sm = 1;
+      if (r.sms < 1) r.sms = 1;
+      return r;
+    }();
+    if (res.err != cudaSuccess) return res.err;
     const int need = (a.ncells + W - 1) / W;
-    const int grid = need < per_sm * sms ? need : per_sm * sms;
+    const int grid = need < res.per_sm * res.sms ? need : res.per_sm * res.sms;
     k2d_step_dyn<S, W, OCC, ATT><<<grid, W * 32, 0, s>>>(a);
     return cudaGetLastError();
   }
