@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "dpm_common.cuh"
@@ -311,8 +312,19 @@ extern "C" int dpm_disperse(dpm_ctx *ctx, int nsystems, const int *ncells, const
   DisperseArgs a{d_begin, d_r, d_L, d_X, d_Y, d_count, d_nb, d_nn, d_inner};
   // positions, starts, radii, U terms and their counts of the largest system
   const size_t smem = sizeof(float) * (5 + kDispTerms + 1) * (size_t)nmax;
-  DPM_CUDA_TRY(cudaFuncSetAttribute(k_disperse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
+  {
+    // the kernel's limit is shared by concurrent calls: only ever raised
+    static std::mutex mu;
+    static size_t granted[64] = {0};
+    int dev = 0;
+    DPM_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || smem > granted[dev]) {
+      DPM_CUDA_TRY(cudaFuncSetAttribute(k_disperse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+      if (dev >= 0 && dev < 64) granted[dev] = smem;
+    }
+  }
   k_disperse<<<nsystems, kDispThreads, smem, s>>>(a);
   DPM_CUDA_TRY(cudaGetLastError());
   DPM_CUDA_TRY(cudaMemcpyAsync(X, d_X, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
