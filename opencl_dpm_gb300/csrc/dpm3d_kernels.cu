@@ -1153,7 +1153,8 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
   const int bx = bin3(gi.cx, T.L, inv, nb), by = bin3(gi.cy, T.L, inv, nb),
             bz = bin3(gi.cz, T.L, inv, nb);
   // lane l finds the sorted range of the l-th neighbouring bin (the
-  // searches run side by side), then the bins are visited in order
+  // searches run side by side), then their cells are tested in bin order,
+  // 32 at a time
   const int lo_off = nb >= 3 ? -1 : 0, hi_off = nb >= 3 ? 1 : nb - 1;
   const int nax = hi_off - lo_off + 1, nbins = nax * nax * nax;  // at most 27
   int blo = 0, bhi = 0;
@@ -1166,17 +1167,30 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
     bhi = lb_u32(a.sorted_keys, blo, T.cell_end, key + 1u);
   }
   int cnt = 0;
-  for (int bin = 0; bin < nbins; ++bin) {
-    const int lo = __shfl_sync(kFull, blo, bin), hi = __shfl_sync(kFull, bhi, bin);
-    for (int b0 = lo; b0 < hi; b0 += 32) {
-      const int q = b0 + lane;
-      const int j = q < hi ? (int)a.sorted_vals[q] : -1;
-      const bool ok = j >= 0 && j != c && pair3(gi, a.geom[j], T);
-      const unsigned m = __ballot_sync(kFull, ok);
-      const int pos = cnt + __popc(m & lt);
-      if (ok && pos < kNb3Buf) buf[w][pos] = j;
-      cnt += __popc(m);
-    }
+  // the bins' cells as one flat range over the lanes (prefix sum of the
+  // bin sizes; a lane finds its bin by binary search over the prefix)
+  const int bsize = bhi - blo;
+  int bincl = bsize;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, bincl, o);
+    if (lane >= o) bincl += y;
+  }
+  const int btotal = __shfl_sync(kFull, bincl, 31);
+  const int bexcl = bincl - bsize;
+  for (int t0 = 0; t0 < btotal; t0 += 32) {
+    const int tt = t0 + lane;
+    int ob = 0;
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1)
+      if (__shfl_sync(kFull, bexcl, ob + st) <= tt) ob += st;
+    const int q = __shfl_sync(kFull, blo, ob) + tt - __shfl_sync(kFull, bexcl, ob);
+    const int j = tt < btotal ? (int)a.sorted_vals[q] : -1;
+    const bool ok = j >= 0 && j != c && pair3(gi, a.geom[j], T);
+    const unsigned m = __ballot_sync(kFull, ok);
+    const int pos = cnt + __popc(m & lt);
+    if (ok && pos < kNb3Buf) buf[w][pos] = j;
+    cnt += __popc(m);
   }
   __syncwarp();
   int nout;
