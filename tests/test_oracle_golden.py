@@ -180,3 +180,20 @@ def test_attraction_3d_live(pbc):
     F = port().attraction3d(s.xyz, s.nv, l0, s.L, pbc, 0.7)
     assert np.count_nonzero(np.abs(ref).sum(1)) > 100
     assert np.linalg.norm(F - ref) <= 1e-6 * np.linalg.norm(ref)
+
+
+def test_attraction_in_the_oracle_step():
+    """The oracle's 3D step adds AllVertAttraction after the other forces when
+    Kat != 0: one step's forces with and without it differ by the
+    attraction alone (up to the rounding of adding it to the other terms)."""
+    from cases import make_tissue3d
+    s = make_tissue3d(5, level=2, phi0=0.5, seed=8)
+    s.Kat = 0.5
+    on, off = s.copy(), s.copy()
+    off.Kat = 0.0
+    Fon, _ = port().run3d(on, 1, 0.005)
+    Foff, _ = port().run3d(off, 1, 0.005)
+    att = port().attraction3d(s.xyz, s.nv, s.l0, s.L, s.pbc, s.Kat)
+    assert np.linalg.norm(att) > 0.1 * np.linalg.norm(Foff)
+    scale = np.abs(Fon).max()
+    assert np.max(np.abs((Fon - Foff) - att)) <= 1e-5 * scale
