@@ -19,7 +19,9 @@ L2 (129 MB) is flushed by writing 256 MB before every timed iteration,
 outside the timed events.  value = vertices * simulation steps / time.
 
 Also reported: the plain single-tissue path on 1,024 bidisperse cells
-("plain"), the dominant kernel's roofline, the end-to-end rate through the C
+("plain"), the 3D monolayer of 256 cells ("plain3d") and 48 smaller
+monolayers in one batch ("batched3d"), the reference's dispersion on the
+device ("disperse"), the dominant kernel's roofline, the end-to-end rate through the C
 ABI with pinned host buffers ("e2e"), the served mixed stream of 2D and 3D
 requests through dpm_serve_* with p50/p99 latency ("served"), SM clocks
 during the timed region and the CPU baseline (the oracle restatement of the
@@ -366,6 +368,8 @@ def run_ours(args, rank, world, local_rank):
              "tuning": ptuned}
 
     p3 = plain3d(ctx, lambda n, fn: timed(None, n, fn), max(3, args.steps))
+    b3 = batched3d(ctx, lambda n, fn: timed(None, n, fn), max(3, args.steps))
+    b3["batched_over_plain"] = round(b3["value"] / p3["value"], 2)
     disp = disperse_leg(ctx, tissues)
 
     served = None
@@ -389,6 +393,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "e2e": e2e, "plain": plain,
         "batched_over_plain": round(value / world / plain["value"], 2),
         "plain3d": p3,
+        "batched3d": b3,
         "disperse": disp,
         "served": served,
         "clocks": clock_info,
@@ -454,6 +459,31 @@ def plain3d(ctx, timed, iters, steps=16):
             "workload": "1 monolayer, 256 cells x 642 vertices (icosphere subdivision 3), "
                         "jittered hexagonal lattice on z=0, kv=1 ka=0.5 ks=0.1 kb=0.05, "
                         "adhesion 0.1, dt=0.002"}
+
+
+def batched3d(ctx, timed, iters, steps=16):
+    """Many independent 3D monolayers in one batch: 48 tissues of N ~
+    U{8..64} cells at subdivision 3 (kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion
+    0.1, dt=0.002), one launch per step for all of them."""
+    from opencl_dpm_gb300 import clDPM
+    from opencl_dpm_gb300.abi import Batch3D
+    rng = np.random.default_rng(5)
+    ts = [build_monolayer(clDPM, rng, int(rng.integers(8, 65)), 3) for _ in range(48)]
+    cat = lambda k: np.concatenate([t[k] for t in ts])
+    b = Batch3D(ctx, [len(t["Kv"]) for t in ts], ts[0]["faces"], ts[0]["nv"])
+    b.set_cells(cat("Kv"), cat("Ka"), cat("Ks"), cat("v0"), cat("a0"), cat("l0"), cat("Kb"),
+                cat("adh"))
+    b.set_tissues([t["L"] for t in ts], 1.0, 1)
+    b.upload(cat("xyz"))
+    for _ in range(3):
+        b.step(steps, DT3)
+    secs = timed(iters, lambda: b.step(steps, DT3))
+    return {"value": round(b.nverts * steps * iters / secs, 1), "unit": UNIT,
+            "ms_per_step": round(secs / iters * 1e3, 4), "sim_steps_per_step": steps,
+            "tissues": len(ts), "cells": int(sum(len(t["Kv"]) for t in ts)),
+            "vertices": int(b.nverts),
+            "workload": "48 monolayers, N ~ U{8..64} cells x 642 vertices (subdivision 3), "
+                        "kv=1 ka=0.5 ks=0.1 kb=0.05, adhesion 0.1, dt=0.002, one batch"}
 
 
 def disperse_leg(ctx, tissues):
