@@ -159,3 +159,16 @@ def test_larger_mesh_after_smaller(ctx):
     r = s3.copy()
     port().run3d(r, 2, DT)
     assert pos_err(x3, r.xyz) <= X_TOL
+
+
+@pytest.mark.parametrize("level", [0, 1])
+def test_coarse_meshes(ctx, level):
+    """Icosahedron (12 vertices) and subdivision 1 (42): a single vertex
+    patch or two, few edges."""
+    s = make_tissue3d(5, level=level, phi0=0.6, seed=20 + level)
+    for nsteps in (1, 10):
+        x, F, wn, rx, rF, rwn = run_case(ctx, s, nsteps)
+        assert wn_mismatch(wn, rwn) <= 2e-2
+        assert pos_err(x, rx) <= X_TOL
+        if nsteps == 1:
+            assert rel_norm_err(F, rF) <= F_TOL
