@@ -140,3 +140,22 @@ def test_checkpoint_keeps_attraction(ctx, tmp_path):
     b2.step(3, DT)
     x2, _ = b2.download()
     assert np.array_equal(x1, x2)
+
+
+def test_checkpoint_without_attraction_section(ctx, tmp_path):
+    """A 3D checkpoint that ends before the attraction section (as files
+    written before it existed) opens with the attraction off."""
+    from opencl_dpm_gb300.abi import Batch3D
+    s = make_tissue3d(3, level=2, phi0=0.5, seed=9)
+    b = gpu_batch3d(ctx, [s])
+    b.step(2, DT)
+    path = tmp_path / "old.ckpt"
+    b.save(str(path))
+    data = path.read_bytes()
+    path.write_bytes(data[:-4 * 1])  # one tissue: drop its Kat
+    b.step(3, DT)
+    x1, _ = b.download()
+    b2 = Batch3D.open(ctx, str(path))
+    b2.step(3, DT)
+    x2, _ = b2.download()
+    assert np.array_equal(x1, x2)
