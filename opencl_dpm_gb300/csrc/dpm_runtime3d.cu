@@ -523,10 +523,9 @@ int dpm3d_set_attraction(dpm3d_batch *b, const float *Kat) {
   if (!Kat) return fail(DPM_EINVAL, "null parameter array");
   if (!b->cells_set || !b->tissues_set)
     return fail(DPM_ESTATE, "set cells and tissues before the attraction");
-  for (int t = 0; t < b->ntissues; ++t) {
+  for (int t = 0; t < b->ntissues; ++t)
     if (!std::isfinite(Kat[t])) return fail(DPM_EINVAL, "Kat must be finite");
-    b->h_tissues[t].Kat = Kat[t];
-  }
+  for (int t = 0; t < b->ntissues; ++t) b->h_tissues[t].Kat = Kat[t];
   b->update_skin();
   cudaSetDevice(b->ctx->device);
   DPM_CUDA_TRY(cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(Tissue3D) * b->ntissues,

@@ -159,3 +159,22 @@ def test_checkpoint_without_attraction_section(ctx, tmp_path):
     b2.step(3, DT)
     x2, _ = b2.download()
     assert np.array_equal(x1, x2)
+
+
+def test_status_codes(ctx):
+    """dpm3d_set_attraction needs the cells and tissues first and a finite
+    strength."""
+    from opencl_dpm_gb300.abi import Batch3D, DPMError
+    s = make_tissue3d(2, level=2, phi0=0.5, seed=1)
+    b = Batch3D(ctx, [s.ncells], s.faces, s.nv)
+    with pytest.raises(DPMError) as e:
+        b.set_attraction([0.5])             # cells and tissues not set
+    assert e.value.code == 5
+    b.set_cells(s.Kv, s.Ka, s.Ks, s.v0, s.a0, s.l0, None, None)
+    b.set_tissues([s.L], [s.Kre], [s.pbc])
+    with pytest.raises(DPMError) as e:
+        b.set_attraction([float("nan")])
+    assert e.value.code == 1
+    b.set_attraction([0.5])
+    b.upload(s.xyz)
+    b.step(1, DT)
