@@ -295,13 +295,29 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
           qy[s2] = pp.y;
         }
       }
+      // one loop over the candidates of every slot (the slot's coordinates
+      // picked by selects): the edge tests are compiled once, not per slot
+      int s = 0;
+      unsigned msk = cm[0];
+      for (;;) {
+        while (!msk && s + 1 < S) {
+          ++s;
 #pragma unroll
-      for (int s = 0; s < S; ++s) {
-        unsigned msk = cm[s];
-        while (msk) {
+          for (int t = 1; t < S; ++t)
+            if (s == t) msk = cm[t];
+        }
+        if (!msk) break;
+        {
           const int l = __ffs(msk) - 1;
           msk &= msk - 1u;
-          const float X = __shfl_sync(kFull, vx[s], l), Y = __shfl_sync(kFull, vy[s], l);
+          float xs = vx[0], ys = vy[0];
+#pragma unroll
+          for (int t = 1; t < S; ++t)
+            if (s == t) {
+              xs = vx[t];
+              ys = vy[t];
+            }
+          const float X = __shfl_sync(kFull, xs, l), Y = __shfl_sync(kFull, ys, l);
           unsigned par = 0u;
           if (far) {
 #pragma unroll
