@@ -51,6 +51,8 @@ UNIT = "vertex-steps/s"
 DT = 0.005
 SIM_STEPS = 32  # simulation steps per benchmark step (a multiple of every rebuild period)
 L2_FLUSH_BYTES = 256 << 20
+WORKLOAD_SWEEP = ("batched 2D sweep: 512 tissues, N~U{8..256}, NV in {16,24,32,48}, "
+                  "kb~LogU[1e-3,1e-1], calA0~U[1,1.3], phi~U[0.6,0.9], ka=kl=kc=1, r0=1, dt=0.005")
 
 
 # ---------------------------------------------------------------------------
@@ -381,9 +383,7 @@ def run_ours(args, rank, world, local_rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded tissues; see config)",
-        "config": {"workload": "batched 2D sweep: 512 tissues, N~U{8..256}, NV in {16,24,32,48}, "
-                               "kb~LogU[1e-3,1e-1], calA0~U[1,1.3], phi~U[0.6,0.9], "
-                               "ka=kl=kc=1, r0=1, dt=0.005",
+        "config": {"workload": WORKLOAD_SWEEP,
                    "tissues": b.ntissues, "cells": N, "vertices": V,
                    "sim_steps_per_step": SIM_STEPS,
                    "l2": "256 MB written before every timed iteration (outside the events)",
@@ -700,7 +700,7 @@ def run_reference(args):
             "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded tissues)",
-            "config": {"workload": "batched 2D sweep (CPU sample)", "sample": desc},
+            "config": {"workload": WORKLOAD_SWEEP, "sample": desc},
             "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores,
                              "kind": "port", "sample": desc},
             "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
