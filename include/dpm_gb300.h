@@ -134,6 +134,17 @@ int dpm2d_diagnostics(dpm2d_batch *b, double *area, double *perimeter,
                       double *energy, double *packing_fraction,
                       double *shape_index);
 
+/* One compression (or expansion) stage on the device: every tissue t with
+ * phi[t] > 0 gets the box side L' = sqrt(sum of cell areas / phi[t]) and
+ * each cell moves rigidly with its vertex-mean centroid scaled by L'/L;
+ * phi[t] == 0 leaves tissue t unchanged.  The same arithmetic, and the same
+ * bits, as the host Tissue2D.SetPackingFraction.  An extension: the
+ * reference fixes L at construction (src/Tissue2D.cpp:31) and has no
+ * compression protocol; this is the quasi-static jamming protocol's box
+ * update without a round trip of the positions through the host.
+ * Synchronizes the batch's stream (the host copy of L is refreshed). */
+int dpm2d_set_packing_fraction(dpm2d_batch *b, const float *phi);
+
 /* State I/O.  dpm2d_device_state returns the DEVICE addresses of the
  * current positions and of the last step's forces (float2 per vertex, the
  * layout of dpm2d_upload), for zero-copy views; they stay valid until the

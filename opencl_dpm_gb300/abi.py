@@ -67,6 +67,7 @@ SIGNATURES = {
                            [ctypes.c_float] * 3 + [ctypes.c_int, _vp, _vp, ctypes.c_int,
                                                    ctypes.c_float, _vp]),
     "dpm2d_diagnostics": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_double)] * 5),
+    "dpm2d_set_packing_fraction": (ctypes.c_int, [_vp, _c_float_p]),
     "dpm2d_device_state": (ctypes.c_int, [_vp] + [ctypes.POINTER(_vp)] * 2),
     "dpm2d_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "dpm2d_open": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
@@ -285,6 +286,13 @@ class Batch2D:
         check(self.lib.dpm2d_diagnostics(self.h, *[x.ctypes.data_as(d) for x in (a, p, e, phi, si)]))
         return {"area": a, "perimeter": p, "energy": e, "packing_fraction": phi,
                 "shape_index": si}
+
+    def set_packing_fraction(self, phi):
+        """Rescales every tissue with phi > 0 to that true packing fraction
+        on the device (box side and centroids; shapes kept); 0 leaves a
+        tissue unchanged."""
+        phi = _f32(np.broadcast_to(phi, (self.ntissues,)))
+        check(self.lib.dpm2d_set_packing_fraction(self.h, fptr(phi)))
 
     def upload(self, xy):
         xy = _f32(xy)

@@ -358,7 +358,82 @@ __global__ void __launch_bounds__(kNbWarps * 32) k2d_neighbors(Rebuild2DArgs a, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Compression: a tissue rescaled to a packing fraction
+// ---------------------------------------------------------------------------
+
+// The host Tissue2D::SetPackingFraction (an extension: the reference has no
+// way to change its box) on the device, with the host's arithmetic so that
+// both give the same bits: each cell's float shoelace area in the
+// reference's order (src/cell.cpp:35-47), summed in double in cell order;
+// L' = sqrt(sum / phi); every vertex moved by its cell's vertex-mean centroid
+// (double) times L'/L - 1 and rounded to float.  One block per tissue;
+// phi <= 0 leaves the tissue as it is.  The tissue's neighbour lists are
+// marked stale (the step scans the whole tissue until the next rebuild).
+__global__ void __launch_bounds__(256)
+    k2d_rescale(const Cell2D *__restrict__ cells, Tissue2D *tissues, const float *phi,
+                float2 *pos, int *stale) {
+  __shared__ float area[256];
+  __shared__ double scale_m1;
+  const int t = blockIdx.x;
+  const float ph = phi[t];
+  if (!(ph > 0.0f)) return;  // the same for the whole block
+  const Tissue2D T = tissues[t];
+  double sum = 0.0;  // thread 0's, in cell order
+  for (int base = T.cell_begin; base < T.cell_end; base += blockDim.x) {
+    const int c = base + (int)threadIdx.x;
+    float a = 0.0f;
+    if (c < T.cell_end) {
+      const Cell2D cp = cells[c];
+      const int n = (int)cp.nv;
+      const float2 *p = pos + cp.voff;
+      for (int i = 0, j = n - 1; i < n; j = i++) {
+        const float s = __fadd_rn(p[j].x, p[i].x), d = __fsub_rn(p[j].y, p[i].y);
+        a = (float)__dadd_rn((double)a, __dmul_rn(0.5, (double)__fmul_rn(s, d)));
+      }
+      a = a < 0.0f ? -a : a;
+    }
+    area[threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int m = min((int)blockDim.x, T.cell_end - base);
+      for (int k = 0; k < m; ++k) sum = __dadd_rn(sum, (double)area[k]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double Lnew = sqrt(__ddiv_rn(sum, (double)ph));
+    scale_m1 = __dsub_rn(__ddiv_rn(Lnew, (double)T.L), 1.0);
+    tissues[t].L = (float)Lnew;
+    stale[t] = 1;
+  }
+  __syncthreads();
+  const double sm1 = scale_m1;
+  for (int c = T.cell_begin + (int)threadIdx.x; c < T.cell_end; c += blockDim.x) {
+    const Cell2D cp = cells[c];
+    const int n = (int)cp.nv;
+    if (n == 0) continue;
+    float2 *p = pos + cp.voff;
+    double cx = 0.0, cy = 0.0;
+    for (int i = 0; i < n; ++i) {
+      cx = __dadd_rn(cx, (double)p[i].x);
+      cy = __dadd_rn(cy, (double)p[i].y);
+    }
+    const double dx = __dmul_rn(__ddiv_rn(cx, (double)n), sm1);
+    const double dy = __dmul_rn(__ddiv_rn(cy, (double)n), sm1);
+    for (int i = 0; i < n; ++i)
+      p[i] = make_float2((float)__dadd_rn((double)p[i].x, dx),
+                         (float)__dadd_rn((double)p[i].y, dy));
+  }
+}
+
 } // namespace
+
+cudaError_t launch_rescale2d(const Cell2D *cells, Tissue2D *tissues, const float *phi,
+                             float2 *pos, int *stale, int ntissues, cudaStream_t s) {
+  k2d_rescale<<<ntissues, 256, 0, s>>>(cells, tissues, phi, pos, stale);
+  return cudaGetLastError();
+}
 
 int bin_axis_count(float L, float w, int cap) {
   int nb = (int)floorf(L / w);

@@ -54,6 +54,10 @@ struct Diag2D {
 };
 cudaError_t launch_diag2d(const Cell2D *cells, const float2 *pos, Diag2D *out, int ncells,
                           cudaStream_t s);
+// Rescales each tissue t with phi[t] > 0 to true packing fraction phi[t]:
+// new L, centroids moved affinely, shapes kept (one block per tissue).
+cudaError_t launch_rescale2d(const Cell2D *cells, Tissue2D *tissues, const float *phi,
+                             float2 *pos, int *stale, int ntissues, cudaStream_t s);
 // Per-tissue bin sizes and per-cell bin keys (one block per tissue).
 cudaError_t launch_binprep2d(const Rebuild2DArgs &a, int local_bits, cudaStream_t s);
 // Neighbour lists from the sorted cell list (one warp per cell).

@@ -91,6 +91,7 @@ struct dpm2d_batch {
   Geom2D *d_geom0 = nullptr;
   int *d_nn = nullptr, *d_nbr = nullptr, *d_stale = nullptr, *d_err = nullptr;
   int *d_sched = nullptr; // dynamic-schedule counters of the step kernel
+  float *d_phi = nullptr; // per-tissue packing fractions of a rescale
   uint32_t *d_keys = nullptr, *d_vals = nullptr, *d_keys_alt = nullptr, *d_vals_alt = nullptr;
   uint32_t *d_sort_scratch = nullptr;
   int cur = 0;
@@ -355,7 +356,8 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     e = A.reserve(sizeof(Cell2D) * N + sizeof(Tissue2D) * ntissues + 3 * sizeof(float2) * V +
                   V + 3 * sizeof(Geom2D) * N + sizeof(int) * (N + N * kMaxNB2D) +
-                  sizeof(int) * (ntissues + 1) + 4 * sizeof(uint32_t) * N +
+                  sizeof(int) * (ntissues + 1) + sizeof(float) * ntissues +
+                  4 * sizeof(uint32_t) * N +
                   radix_sort_scratch_bytes((int)N) + 64 * 256);
     if (e != cudaSuccess) return cuda_fail(e, "device allocation");
     b->d_cells = A.take<Cell2D>(N);
@@ -372,6 +374,7 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     b->d_stale = A.take<int>(ntissues);
     b->d_err = A.take<int>(1);
     b->d_sched = A.take<int>(2);
+    b->d_phi = A.take<float>(ntissues);
     b->d_keys = A.take<uint32_t>(N);
     b->d_vals = A.take<uint32_t>(N);
     b->d_keys_alt = A.take<uint32_t>(N);
@@ -706,6 +709,40 @@ int dpm2d_cell_areas(dpm2d_batch *b, float *area) {
                                cudaMemcpyDeviceToHost, b->stream));
   DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
   for (int c = 0; c < b->ncells; ++c) area[c] = g[c].area;
+  return DPM_OK;
+}
+
+int dpm2d_set_packing_fraction(dpm2d_batch *b, const float *phi) {
+  if (int r = check_batch(b)) return r;
+  if (!phi) return fail(DPM_EINVAL, "null packing fractions");
+  if (!b->uploaded || !b->cells_set || !b->tissues_set)
+    return fail(DPM_ESTATE, "set cells and tissues and upload positions before rescaling");
+  bool any = false;
+  for (int t = 0; t < b->ntissues; ++t) {
+    if (!(phi[t] >= 0.0f) || !std::isfinite(phi[t]))
+      return fail(DPM_EINVAL, "packing fractions must be finite and non-negative (0: unchanged)");
+    any |= phi[t] > 0.0f;
+  }
+  if (!any) return DPM_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStream_t s = b->stream;
+  DPM_CUDA_TRY(cudaMemcpyAsync(b->d_phi, phi, sizeof(float) * b->ntissues,
+                               cudaMemcpyHostToDevice, s));
+  DPM_CUDA_TRY(launch_rescale2d(b->d_cells, b->d_tissues, b->d_phi, b->d_pos[b->cur],
+                                b->d_stale, b->ntissues, s));
+  DPM_CUDA_TRY(launch_geom2d(b->d_cells, b->d_pos[b->cur], b->d_geom[b->cur], b->ncells,
+                             b->maxnv, s));
+  // the host copy of each box side follows the device's
+  std::vector<Tissue2D> dev(b->ntissues);
+  DPM_CUDA_TRY(cudaMemcpyAsync(dev.data(), b->d_tissues, sizeof(Tissue2D) * b->ntissues,
+                               cudaMemcpyDeviceToHost, s));
+  DPM_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int t = 0; t < b->ntissues; ++t) {
+    if (!(phi[t] > 0.0f)) continue;
+    if (!(dev[t].L > 0.0f) || !std::isfinite(dev[t].L))
+      return fail(DPM_ENONFINITE, "rescaled box side is not finite");
+    b->h_tissues[t].L = dev[t].L;
+  }
   return DPM_OK;
 }
 

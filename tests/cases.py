@@ -55,6 +55,44 @@ def make_tissue2d(ncells=16, nv=32, r0=1.0, calA=1.0, Ka=1.0, Kl=1.0, Kb=0.0, ph
                          L=float(L), Kre=float(Kre), Kat=float(Kat), pbc=pbc)
 
 
+def rescale_packing(state: Tissue2DState, phi: float) -> Tissue2DState:
+    """The host Tissue2D.SetPackingFraction restated with numpy, operation by
+    operation (float32 where it rounds to float, float64 where it promotes):
+    per cell the float shoelace area with a double accumulator, summed in
+    double in cell order; L' = sqrt(sum / phi); each cell shifted by its
+    double vertex-mean centroid times (L'/L - 1).  Returns a new state."""
+    s = state.copy()
+    f32, f64 = np.float32, np.float64
+    off = s.off
+    nv = s.nv.astype(np.int64)
+    xy = s.xy.astype(f32)
+    areas = np.zeros(len(nv), f32)
+    cents = np.zeros((len(nv), 2), f64)
+    for n in np.unique(nv):
+        cells = np.nonzero(nv == n)[0]
+        idx = off[cells][:, None].astype(np.int64) + np.arange(n)[None, :]
+        x, y = xy[idx, 0], xy[idx, 1]
+        a = np.zeros(len(cells), f32)
+        j = n - 1
+        for i in range(n):
+            sm = x[:, j] + x[:, i]
+            d = y[:, j] - y[:, i]
+            a = (a.astype(f64) + 0.5 * (sm * d).astype(f64)).astype(f32)
+            j = i
+        areas[cells] = np.abs(a)
+        # sequential double sums over each ring (accumulate is in order)
+        cents[cells, 0] = np.add.accumulate(x.astype(f64), axis=1)[:, -1] / f64(n)
+        cents[cells, 1] = np.add.accumulate(y.astype(f64), axis=1)[:, -1] / f64(n)
+    total = float(np.add.accumulate(areas.astype(f64))[-1])
+    Lnew = np.sqrt(total / f64(f32(phi)))
+    sm1 = Lnew / f64(f32(s.L)) - 1.0
+    shift = cents * sm1
+    rep = np.repeat(shift, nv, axis=0)
+    s.xy = (xy.astype(f64) + rep).astype(f32)
+    s.L = float(f32(Lnew))
+    return s
+
+
 def perturb(state: Tissue2DState, scale: float, seed: int) -> Tissue2DState:
     s = state.copy()
     rng = np.random.default_rng(seed)

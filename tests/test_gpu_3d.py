@@ -4,8 +4,10 @@ Tolerances (FP32):
   * forces of one step from the same positions: ||F - F_ref|| <= 1e-5 ||F_ref||
   * positions after N steps: max |x - x_ref| / max(|x_ref|, 1) <= 1e-4
   * winding-number hit counts: equal, except where the oracle's own sum sits
-    at the reference's 1e-6 threshold by rounding noise (at most 0.2% of
-    vertices may differ; their force contribution is ~1e-6 * Kc).
+    at the reference's 1e-6 threshold by rounding noise: at most 0.2% of the
+    vertices may differ, and at least one is always allowed (a 5-cell tissue
+    of icosahedra has 60 vertices, where 0.2% is less than one); their force
+    contribution is ~1e-6 * Kc.
 """
 import numpy as np
 import pytest
@@ -44,8 +46,10 @@ def run_case(ctx, state, nsteps, tuning=None):
     return x, F, wn, rx, rF, rwn
 
 
-def wn_mismatch(a, b):
-    return float(np.mean(a != b))
+def wn_ok(a, b):
+    """Hit counts equal except on at most max(1, 0.2% of the vertices)."""
+    bad = int(np.count_nonzero(a != b))
+    return bad <= max(1, int(2e-3 * a.size)), bad
 
 
 @pytest.mark.parametrize("seed", [0, 1])
@@ -53,7 +57,7 @@ def test_one_step_level2(ctx, seed):
     s = make_tissue3d(6, level=2, phi0=0.5, seed=seed)
     x, F, wn, rx, rF, rwn = run_case(ctx, s, 1)
     assert rwn.sum() > 0  # the cells overlap: repulsion is exercised
-    assert wn_mismatch(wn, rwn) <= 2e-3
+    assert wn_ok(wn, rwn)[0], wn_ok(wn, rwn)
     assert rel_norm_err(F, rF) <= F_TOL
     assert pos_err(x, rx) <= X_TOL
 
@@ -76,7 +80,7 @@ def test_level3(ctx):
     s = make_tissue3d(4, level=3, phi0=0.5, seed=4)
     x, F, wn, rx, rF, rwn = run_case(ctx, s, 1)
     assert rel_norm_err(F, rF) <= F_TOL
-    assert wn_mismatch(wn, rwn) <= 2e-3
+    assert wn_ok(wn, rwn)[0], wn_ok(wn, rwn)
     x, F, wn, rx, rF, rwn = run_case(ctx, s, 10)
     assert pos_err(x, rx) <= X_TOL
 
@@ -140,7 +144,7 @@ def test_monolayer_level3_contacts(ctx):
     for nsteps in (1, 10):
         x, F, wn, rx, rF, rwn = run_case(ctx, s, nsteps)
         assert rwn.sum() > 100  # many vertices inside a neighbour
-        assert wn_mismatch(wn, rwn) <= 2e-3
+        assert wn_ok(wn, rwn)[0], wn_ok(wn, rwn)
         assert pos_err(x, rx) <= X_TOL
         if nsteps == 1:
             assert rel_norm_err(F, rF) <= F_TOL
@@ -168,7 +172,7 @@ def test_coarse_meshes(ctx, level):
     s = make_tissue3d(5, level=level, phi0=0.6, seed=20 + level)
     for nsteps in (1, 10):
         x, F, wn, rx, rF, rwn = run_case(ctx, s, nsteps)
-        assert wn_mismatch(wn, rwn) <= 2e-2
+        assert wn_ok(wn, rwn)[0], wn_ok(wn, rwn)
         assert pos_err(x, rx) <= X_TOL
         if nsteps == 1:
             assert rel_norm_err(F, rF) <= F_TOL
