@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 DPM step (one JSON line on stdout).
 
-Workload (default, the batched 2D sweep): 512 independent tissues with
+Headline workload, the batched 2D sweep: 512 independent tissues with
 N ~ U{8..256} cells and NV ~ {16, 24, 32, 48} vertices per cell (one NV per
 tissue), per-tissue kb ~ LogU[1e-3, 1e-1], calA0 ~ U[1.0, 1.3], true packing
 fraction ~ U[0.6, 0.9] (phi0 = sqrt(phi)), ka = kl = kc = 1, r0 = 1,
@@ -9,26 +9,34 @@ dt = 0.005.  Cells start as the Cell2D constructor's regular polygons, centred
 on a seeded, jittered square lattice of the tissue's periodic box (synthetic
 data; the reference names no dataset).  All tissues step together in one
 batch; each simulation step is one launch of the fused step kernel, and the
-neighbour-list rebuild plus one rebuild period of steps (8, 16 or 32, chosen
-with warps per block and the register variant by the project's autotuner,
+neighbour-list rebuild plus one rebuild period of steps (chosen with warps
+per block and the kernel variant by the project's autotuner,
 dpm2d_autotune) are one captured CUDA graph.
 
 One benchmark "step" is one dpm2d_step call of 32 simulation steps of the
-whole batch.
-L2 (129 MB) is flushed by writing 256 MB before every timed iteration,
-outside the timed events.  value = vertices * simulation steps / time.
+whole batch.  L2 (129 MB) is flushed by writing 256 MB before every timed
+iteration, outside the timed events.  value = vertices * simulation steps /
+time.
 
-Also reported: the plain single-tissue path on 1,024 bidisperse cells
-("plain"), the 3D monolayer of 256 cells ("plain3d") and 48 smaller
-monolayers in one batch ("batched3d"), the reference's dispersion on the
-device ("disperse"), the dominant kernel's roofline, the end-to-end rate through the C
-ABI with pinned host buffers ("e2e"), the served mixed stream of 2D and 3D
-requests through dpm_serve_* with p50/p99 latency ("served"), SM clocks
-during the timed region and the CPU baseline (the oracle restatement of the
-reference on the host cores).
+Also reported (keys of the same line): the plain single-system paths -- the
+1,024-cell compression protocol ("plain"), the 16-cell run of 10,000 steps
+("plain_c0"), the 256-cell 3D monolayer ("plain3d") -- 48 monolayers in one
+batch ("batched3d"), the same 32-tissue sample the reference arm times
+("same_sample"), the sweep's full 20,000-step run ("steady_state"), the
+reference's dispersion on the device ("disperse"), the dominant kernel's HBM
+and issue rooflines, the end-to-end rate through the C ABI with pinned host
+buffers ("e2e"), the served mixed stream of 2D and 3D requests through
+dpm_serve_* with p50/p99 latency ("served"), SM clocks during the timed
+region, and CPU baselines (the oracle restatement of the reference on the
+host cores, single-thread and all-core).
+
+The GPU arm builds its inputs with the product's own host model (clDPM); the
+reference arm (--impl reference) builds the same inputs with the oracle and
+never imports the product.  Both builders give the same bits
+(tests/test_bench_workloads.py).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--serve-requests R]
+                  [--serve-requests R] [--cpu-budget S]
 """
 from __future__ import annotations
 
@@ -50,13 +58,57 @@ METRIC = "vertex-steps/s batched+served vs plain on 1 GB300; p50/p99 run latency
 UNIT = "vertex-steps/s"
 DT = 0.005
 SIM_STEPS = 32  # simulation steps per benchmark step (a multiple of every rebuild period)
+SWEEP_SEED = 1000
+SAMPLE_EVERY = 16  # the CPU sample: every 16th tissue of the sweep
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD_SWEEP = ("batched 2D sweep: 512 tissues, N~U{8..256}, NV in {16,24,32,48}, "
                   "kb~LogU[1e-3,1e-1], calA0~U[1,1.3], phi~U[0.6,0.9], ka=kl=kc=1, r0=1, dt=0.005")
+L2_NOTE = "256 MB written before every timed iteration of the GPU arm (outside the events)"
 
 
 # ---------------------------------------------------------------------------
-# workloads (built with the product's own host model, clDPM)
+# geometry providers
+# ---------------------------------------------------------------------------
+
+class ProductGeometry:
+    """Cells and boxes from the product's host model (clDPM): the GPU arm."""
+
+    def __init__(self):
+        from opencl_dpm_gb300 import clDPM
+        self.m = clDPM
+
+    def tissue2d(self, calA, nv, r0, phi0):
+        """Regular polygons at the origin, their rest area and edge, and the
+        box of the Tissue2D constructor (L = sqrt(sum A) / phi0)."""
+        proto = [self.m.Cell2D(0.0, 0.0, float(calA[i]), int(nv[i]), float(r0[i]))
+                 for i in range(len(nv))]
+        L = self.m.Tissue2D(proto, float(phi0)).L
+        return ([np.asarray(p.Verts, np.float32) for p in proto],
+                np.float32([p.a0 for p in proto]), np.float32([p.l0 for p in proto]),
+                np.float32(L))
+
+
+class OracleGeometry:
+    """The same from the oracle (oracle/): the reference arm, which must not
+    load the product."""
+
+    def __init__(self):
+        from oracle.oracle import Port
+        self.P = Port()
+
+    def tissue2d(self, calA, nv, r0, phi0):
+        xs, a0, l0, areas = [], [], [], []
+        for i in range(len(nv)):
+            xy, a, l, _ = self.P.cell2d(0.0, 0.0, float(calA[i]), int(nv[i]), float(r0[i]))
+            xs.append(xy)
+            a0.append(a)
+            l0.append(l)
+            areas.append(self.P.area2d(xy))
+        return xs, np.float32(a0), np.float32(l0), np.float32(self.P.box2d(areas, float(phi0)))
+
+
+# ---------------------------------------------------------------------------
+# workloads
 # ---------------------------------------------------------------------------
 
 def lattice_centres(rng, n, L, jitter=0.1):
@@ -69,54 +121,72 @@ def lattice_centres(rng, n, L, jitter=0.1):
     return c.astype(np.float32)
 
 
-def build_tissue(clDPM, rng, n, nv, calA, r0, Kb, phi):
-    """One tissue: regular polygons at lattice centres; returns arrays."""
-    proto = [clDPM.Cell2D(0.0, 0.0, float(calA[i]), int(nv[i]), float(r0[i])) for i in range(n)]
-    T = clDPM.Tissue2D(proto, float(np.sqrt(phi)))
-    L = T.L
-    cen = lattice_centres(rng, n, L)
-    xy, a0, l0 = [], [], []
-    for i, p in enumerate(proto):
-        v = np.asarray(p.Verts, np.float32) + cen[i]
-        xy.append(v)
-        a0.append(p.a0)
-        l0.append(p.l0)
-    return dict(nv=np.asarray(nv, np.uint32), xy=np.concatenate(xy), a0=np.float32(a0),
-                l0=np.float32(l0), r0=np.asarray(r0, np.float32),
-                Ka=np.ones(n, np.float32), Kl=np.ones(n, np.float32),
-                Kb=np.full(n, Kb, np.float32), L=np.float32(L), Kre=1.0, Kat=0.0)
+def build_tissue(geo, rng, n, nv, calA, r0, Kb, phi, centres="lattice"):
+    """One tissue: regular polygons at jittered lattice (or uniform) centres."""
+    polys, a0, l0, L = geo.tissue2d(calA, nv, r0, np.sqrt(phi))
+    if centres == "lattice":
+        cen = lattice_centres(rng, n, L)
+    else:
+        cen = rng.uniform(0.0, L, size=(n, 2)).astype(np.float32)
+    xy = np.concatenate([polys[i] + cen[i] for i in range(n)])
+    return dict(nv=np.asarray(nv, np.uint32), xy=xy, a0=a0, l0=l0,
+                r0=np.asarray(r0, np.float32), Ka=np.ones(n, np.float32),
+                Kl=np.ones(n, np.float32), Kb=np.full(n, Kb, np.float32), L=L, Kre=1.0,
+                Kat=0.0)
 
 
-def workload_batched(seed=0, ntissues=512):
-    from opencl_dpm_gb300 import clDPM
+def workload_batched(geo, seed=SWEEP_SEED, ntissues=512):
     rng = np.random.default_rng(seed)
     tissues = []
-    for t in range(ntissues):
+    for _ in range(ntissues):
         n = int(rng.integers(8, 257))
         nv = int(rng.choice([16, 24, 32, 48]))
         kb = float(10 ** rng.uniform(-3, -1))
         calA = rng.uniform(1.0, 1.3, n)
         phi = float(rng.uniform(0.6, 0.9))
-        tissues.append(build_tissue(clDPM, rng, n, np.full(n, nv), calA, np.ones(n), kb, phi))
+        tissues.append(build_tissue(geo, rng, n, np.full(n, nv), calA, np.ones(n), kb, phi))
     return tissues
 
 
-def workload_plain(seed=1, n=1024):
-    from opencl_dpm_gb300 import clDPM
+def workload_c1(geo, seed=1, n=1024):
+    """1,024 cells x 32 vertices, bidisperse r0 1.0 / 1.4 (shuffled), calA0 ~
+    U[1, 1.2], kb = 0.01, at true packing fraction 0.6."""
     rng = np.random.default_rng(seed)
     r0 = rng.permutation(np.r_[np.full(n // 2, 1.0), np.full(n - n // 2, 1.4)])
     calA = rng.uniform(1.0, 1.2, n)
-    return [build_tissue(clDPM, rng, n, np.full(n, 32), calA, r0, 0.01, 0.6)]
+    return [build_tissue(geo, rng, n, np.full(n, 32), calA, r0, 0.01, 0.6)]
+
+
+def workload_c0(geo, seed=2):
+    """16 cells x 32 vertices, calA0 = 1, kb = 0, uniform random centres at
+    true packing fraction 0.6."""
+    rng = np.random.default_rng(seed)
+    return [build_tissue(geo, rng, 16, np.full(16, 32), np.ones(16), np.ones(16), 0.0, 0.6,
+                         centres="uniform")]
+
+
+def sweep_sample(tissues):
+    return tissues[::SAMPLE_EVERY]
+
+
+def sample_desc(tissues):
+    s = sweep_sample(tissues)
+    return (f"{len(s)} of {len(tissues)} tissues (every {SAMPLE_EVERY}th, "
+            f"{sum(int(t['nv'].sum()) for t in s)} vertices)")
 
 
 DT3 = 0.002  # 3D monolayer time step
 
 
-def build_monolayer(clDPM, rng, n, level, r0=1.0, calA=1.05):
+def build_monolayer(clDPM, rng, n, level, r0=1.0):
     """n icospheres (Cell3D ctor geometry) resting on z = 0, centres on a
     jittered hexagonal lattice (spacing 2 r0, jitter U[-0.1, 0.1]) in a
-    periodic box; kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion range 0.1."""
-    proto = clDPM.Cell3D([0.0, 0.0, 0.0], calA, r0, level)
+    periodic box; kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion range 0.1.  Target
+    volume 1.0x the initial mesh volume; target area 1.05x the initial true
+    mesh area (the constructor's SurfaceArea is twice the area), spread over
+    the faces, with the rest edge from it by the reference's rule
+    l0 = sqrt(4 a0) / sqrt(3)."""
+    proto = clDPM.Cell3D([0.0, 0.0, 0.0], 1.0, r0, level)
     ring = np.asarray(proto.Verts, np.float32)
     faces = np.asarray(proto.GetFaces(), np.uint32)
     m = int(math.ceil(math.sqrt(n)))
@@ -128,13 +198,18 @@ def build_monolayer(clDPM, rng, n, level, r0=1.0, calA=1.05):
     cy = (iy + 0.5) * sp + rng.uniform(-0.1, 0.1, n)
     cen = np.stack([cx, cy, np.full(n, r0)], axis=1).astype(np.float32)
     xyz = np.concatenate([ring + cen[i] for i in range(n)])
-    a0 = np.full(n, proto.a0, np.float32)
+    v0 = np.float32(proto.Volume)
+    a_face = np.float32(1.05 * (0.5 * float(proto.SurfaceArea)) / int(proto.NF))
+    a0 = np.full(n, a_face, np.float32)
     # the host model's rest edge: sqrt(double(4 a0)) / sqrt(3), 4 a0 in float
     l0 = (np.sqrt((np.float32(4.0) * a0).astype(np.float64)) / np.sqrt(3.0)).astype(np.float32)
     f = lambda v: np.full(n, v, np.float32)
     return dict(dim=3, nv=int(proto.NV), faces=faces, xyz=xyz, Kv=f(1.0), Ka=f(0.5), Ks=f(0.1),
-                v0=f(proto.v0), a0=a0, l0=l0, Kb=f(0.05), adh=f(0.1), L=L, Kre=1.0,
-                level=level)
+                v0=f(v0), a0=a0, l0=l0, Kb=f(0.05), adh=f(0.1), L=L, Kre=1.0, level=level)
+
+
+C2_NOTE = ("kv=1 ka=0.5 ks=0.1 kb=0.05, adhesion range 0.1, v0 = initial mesh volume, "
+           "target area 1.05x the initial mesh area, dt=0.002")
 
 
 def make_batch(ctx, tissues):
@@ -147,6 +222,17 @@ def make_batch(ctx, tissues):
     xy = cat("xy")
     b.upload(xy)
     return b, xy
+
+
+def make_batch3d(ctx, ts):
+    from opencl_dpm_gb300.abi import Batch3D
+    cat = lambda k: np.concatenate([t[k] for t in ts])
+    b = Batch3D(ctx, [len(t["Kv"]) for t in ts], ts[0]["faces"], ts[0]["nv"])
+    b.set_cells(cat("Kv"), cat("Ka"), cat("Ks"), cat("v0"), cat("a0"), cat("l0"), cat("Kb"),
+                cat("adh"))
+    b.set_tissues([t["L"] for t in ts], 1.0, 1)
+    b.upload(cat("xyz"))
+    return b
 
 
 # ---------------------------------------------------------------------------
@@ -218,19 +304,34 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(summary):
-    """DRAM bytes (read + write) per launch from the committed ncu summary
-    `profiles/<summary>.md` (its "traffic (read + write) per launch" row)."""
+def profile_rows(summary):
+    """Rows of the committed ncu summary `profiles/<summary>.md`: the
+    'traffic (read + write) per launch' and 'warp instructions per launch'
+    figures and the build the capture was taken of."""
     p = os.path.join(ROOT, "profiles", summary + ".md")
+    out = {"traffic": None, "warp_inst": None, "build": None}
+    units = {"MB": 1e6, "GB": 1e9, "KB": 1e3, "M": 1e6, "G": 1e9, "k": 1e3}
     try:
         with open(p) as f:
             for line in f:
-                if line.startswith("| traffic (read + write) per launch"):
-                    v, unit = line.split("|")[2].split()
-                    return float(v) * {"MB": 1e6, "GB": 1e9, "KB": 1e3}[unit]
-    except (OSError, ValueError, KeyError, IndexError):
+                cells = [c.strip() for c in line.split("|")]
+                if len(cells) < 3:
+                    continue
+                key = cells[1]
+                try:
+                    if key.startswith("traffic (read + write) per launch"):
+                        v, unit = cells[2].split()[:2]
+                        out["traffic"] = float(v) * units[unit]
+                    elif key.startswith("warp instructions per launch"):
+                        v, unit = cells[2].split()[:2]
+                        out["warp_inst"] = float(v) * units[unit]
+                    elif key.startswith("build captured"):
+                        out["build"] = cells[2]
+                except (ValueError, KeyError):
+                    pass
+    except OSError:
         pass
-    return None
+    return out
 
 
 def launches_per_call(batch, sim_steps, period):
@@ -260,6 +361,48 @@ def reduce_over_ranks(secs, units, world, device):
     return float(t.item()), float(u.item())
 
 
+class Timer:
+    """CUDA-event timing on the context's stream, L2 flushed before each
+    iteration (outside the events)."""
+
+    def __init__(self, ctx, device):
+        import torch
+        self.torch = torch
+        self.ctx = ctx
+        self.stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+        self.flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
+                                 device=f"cuda:{device}")
+
+    def __call__(self, iters, fn, flush=True):
+        """Seconds per iteration (mean)."""
+        torch = self.torch
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(iters)]
+        with torch.cuda.stream(self.stream):
+            for i in range(iters):
+                if flush:
+                    self.flush.zero_()
+                ev[i][0].record(self.stream)
+                fn()
+                ev[i][1].record(self.stream)
+        torch.cuda.synchronize()
+        self.ctx.synchronize()
+        return sum(s.elapsed_time(e) for s, e in ev) / iters / 1e3
+
+    def span(self, fn):
+        """Seconds of fn() between two events on the stream (fn may
+        synchronize the stream itself)."""
+        torch = self.torch
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(self.stream):
+            a.record(self.stream)
+            out = fn()
+            b.record(self.stream)
+        torch.cuda.synchronize()
+        self.ctx.synchronize()
+        return a.elapsed_time(b) / 1e3, out
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -270,29 +413,13 @@ def run_ours(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     ctx = Context(local_rank)
-    stream = torch.cuda.ExternalStream(ctx.stream(), device=local_rank)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+    timed = Timer(ctx, local_rank)
+    geo = ProductGeometry()
 
-    tissues = workload_batched(seed=1000 + rank)
+    tissues = workload_batched(geo, seed=SWEEP_SEED + rank)
     b, xy_host = make_batch(ctx, tissues)
     V, N = b.nverts, b.ncells
     tuned = b.autotune(DT, trial_blocks=2, use_cache=True)
-
-    def timed(batch, iters, fn):
-        total = 0.0
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(iters)]
-        with torch.cuda.stream(stream):
-            for i in range(iters):
-                flush.zero_()
-                ev[i][0].record(stream)
-                fn()
-                ev[i][1].record(stream)
-        torch.cuda.synchronize()
-        ctx.synchronize()
-        for s, e in ev:
-            total += s.elapsed_time(e)
-        return total / 1e3
 
     for _ in range(max(3, args.warmup)):
         b.step(SIM_STEPS, DT)
@@ -304,7 +431,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     clocks = ClockSampler(local_rank)
     clocks.start()
-    secs = timed(b, args.steps, lambda: b.step(SIM_STEPS, DT))
+    secs = timed(args.steps, lambda: b.step(SIM_STEPS, DT)) * args.steps
     clock_info = clocks.stop()
     torch.cuda.synchronize()
     secs, units = reduce_over_ranks(secs, float(V) * SIM_STEPS * args.steps, world,
@@ -315,22 +442,96 @@ def run_ours(args, rank, world, local_rank):
     if rank != 0:
         return None
 
-    # dominant kernel: the fused step, launched alone after a flush
+    roofline = step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info)
+    e2e = e2e_leg(b, timed, V, args)
+    sample = same_sample_leg(ctx, timed, tissues, args)
+
+    c1 = plain_c1(ctx, timed, geo)
+    c0 = plain_c0(ctx, timed, geo)
+    p3 = plain3d(ctx, timed, max(3, args.steps))
+    b3 = batched3d(ctx, timed, max(3, args.steps))
+    b3["batched_over_plain"] = round(b3["value"] / p3["value"], 2)
+    steady = steady_state_leg(ctx, timed, geo)
+    disp = disperse_leg(ctx, tissues, geo)
+
+    served = None
+    if args.serve_requests > 0:
+        served = run_served(ctx, args.serve_requests, plain2d=c1["value"], plain3d=p3["value"])
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded tissues; see config)",
+        "config": sweep_config(b.ntissues, N, V),
+        "graph": "one CUDA graph replay per cell-list rebuild period",
+        "tuning": tuned,
+        "gpu_launches": launches_per_call(b, SIM_STEPS, tuned["rebuild_period"]) * args.steps,
+        "roofline": roofline, "e2e": e2e, "same_sample": sample,
+        "plain": c1,
+        "batched_over_plain": round(value / world / c1["value"], 2),
+        "plain_c0": c0,
+        "plain3d": p3,
+        "batched3d": b3,
+        "steady_state": steady,
+        "disperse": disp,
+        "served": served,
+        "clocks": clock_info,
+    }
+    line["cpu_baseline"] = cpu_baseline(tissues, budget_s=args.cpu_budget)
+    line["cpu_baselines"] = cpu_baselines_plain(geo, args.cpu_budget)
+    return line
+
+
+def sweep_config(ntissues, ncells, nverts):
+    """The workload both arms name (identical on both)."""
+    return {"workload": WORKLOAD_SWEEP, "tissues": ntissues, "cells": ncells,
+            "vertices": nverts, "seed": SWEEP_SEED, "sim_steps_per_step": SIM_STEPS,
+            "l2": L2_NOTE}
+
+
+def step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info):
+    """HBM and issue rooflines of the fused step kernel (k2d_step)."""
+    # one launch at a time after an L2 flush (cold), and the kernel's share
+    # of the graph: the graph's time per simulation step less the rebuild
     nk = 20
-    kern = timed(b, nk, lambda: b.step_kernel(DT)) / nk
+    kern = timed(nk, lambda: b.step_kernel(DT))
+    rebuild_s, _ = timed.span(b.rebuild_now)
+    period = tuned["rebuild_period"]
+    in_graph = (ms_per_step / 1e3 - rebuild_s * SIM_STEPS / period) / SIM_STEPS
     bytes_per_launch = 16.0 * V + 28.0 * N
     peak, peak_kind = measured_peak_hbm()
-    achieved = bytes_per_launch / kern / 1e9
-    traffic = profiled_traffic("k2d_step_batched512")
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS)",
-                "kernel": "k2d_step", "kernel_us": round(kern * 1e6, 2),
-                "bytes_per_launch": int(bytes_per_launch),
-                "traffic": None if traffic is None else int(traffic)}
+    achieved = bytes_per_launch / in_graph / 1e9
+    prof = profile_rows("k2d_step_batched512")
+    sm_mhz = clock_info.get("sm_mhz") or 2070.0
+    issue = None
+    if prof["warp_inst"]:
+        slots = 152 * 4 * sm_mhz * 1e6 * in_graph
+        issue = {"warp_inst_per_launch": int(prof["warp_inst"]),
+                 "issue_slots_per_launch": int(slots), "frac": round(prof["warp_inst"] / slots, 4),
+                 "formula": "warp instructions / (152 SMs x 4 schedulers x SM clock x in-graph "
+                            "launch time)",
+                 "source": "profiles/k2d_step_batched512.md (ncu, build " +
+                           str(prof["build"]) + ")"}
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS)",
+            "kernel": "k2d_step", "in_graph_us": round(in_graph * 1e6, 2),
+            "cold_single_launch_us": round(kern * 1e6, 2),
+            "cold_frac": round(bytes_per_launch / kern / 1e9 / peak, 4),
+            "rebuild_us": round(rebuild_s * 1e6, 2),
+            "bytes_per_launch": int(bytes_per_launch),
+            "traffic": None if prof["traffic"] is None else int(prof["traffic"]),
+            "traffic_source": "profiles/k2d_step_batched512.md (ncu dram__bytes_read.sum + "
+                              "dram__bytes_write.sum of one launch, build " +
+                              str(prof["build"]) + ")",
+            "issue": issue}
 
-    # end to end through the C ABI: pinned host in, stepped, pinned host out;
-    # the input is the batch's current (relaxed) state, so the device work
-    # per step matches the timed region
+
+def e2e_leg(b, timed, V, args):
+    """End to end through the C ABI: pinned host in, stepped, pinned host
+    out; the input is the batch's current (relaxed) state, so the device work
+    per step matches the timed region."""
+    import torch
     xy_now, _ = b.download()
     xy_pin = torch.from_numpy(np.ascontiguousarray(xy_now.reshape(-1))).pin_memory()
     out_pin = torch.empty_like(xy_pin).pin_memory()
@@ -347,146 +548,142 @@ def run_ours(args, rank, world, local_rank):
     # after their copies complete), L2 flushed before each iteration
     tt = 0.0
     for _ in range(e_iters):
-        flush.zero_()
+        timed.flush.zero_()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         e2e_once()
         tt += time.perf_counter() - t1
-    e2e = {"value": round(V * SIM_STEPS * e_iters / tt, 1), "unit": UNIT,
-           "h2d_bytes_per_step": int(8 * V), "d2h_bytes_per_step": int(16 * V),
-           "path": "dpm2d_upload + dpm2d_step(32) + dpm2d_download, pinned host buffers"}
+    return {"value": round(V * SIM_STEPS * e_iters / tt, 1), "unit": UNIT,
+            "h2d_bytes_per_step": int(8 * V), "d2h_bytes_per_step": int(16 * V),
+            "path": "dpm2d_upload + dpm2d_step(32) + dpm2d_download, pinned host buffers"}
 
-    # plain single-tissue path (1,024 cells) for the batched/plain ratio
-    pt = workload_plain()
-    pb, _ = make_batch(ctx, pt)
-    ptuned = pb.autotune(DT, trial_blocks=2, use_cache=True)
+
+def same_sample_leg(ctx, timed, tissues, args):
+    """The 32 tissues the reference arm times, alone as one batch."""
+    ts = sweep_sample(tissues)
+    b, _ = make_batch(ctx, ts)
+    tuned = b.autotune(DT, trial_blocks=2, use_cache=True)
     for _ in range(3):
-        pb.step(SIM_STEPS, DT)
-    p_secs = timed(pb, max(3, args.steps), lambda: pb.step(SIM_STEPS, DT))
-    plain = {"value": round(pb.nverts * SIM_STEPS * max(3, args.steps) / p_secs, 1),
-             "unit": UNIT, "ms_per_step": round(p_secs / max(3, args.steps) * 1e3, 4),
-             "workload": "1 tissue, 1024 cells x 32 vertices, bidisperse r0 1.0/1.4, "
-                         "calA0 ~ U[1.0,1.2], kb=0.01, packing fraction 0.6 (static box)",
-             "tuning": ptuned}
-
-    p3 = plain3d(ctx, lambda n, fn: timed(None, n, fn), max(3, args.steps))
-    b3 = batched3d(ctx, lambda n, fn: timed(None, n, fn), max(3, args.steps))
-    b3["batched_over_plain"] = round(b3["value"] / p3["value"], 2)
-    disp = disperse_leg(ctx, tissues)
-
-    served = None
-    if args.serve_requests > 0:
-        served = run_served(ctx, args.serve_requests)
-
-    line = {
-        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded tissues; see config)",
-        "config": {"workload": WORKLOAD_SWEEP,
-                   "tissues": b.ntissues, "cells": N, "vertices": V,
-                   "sim_steps_per_step": SIM_STEPS,
-                   "l2": "256 MB written before every timed iteration (outside the events)",
-                   "graph": "one CUDA graph replay per cell-list rebuild period",
-                   "tuning": tuned},
-        "gpu_launches": launches_per_call(b, SIM_STEPS, tuned["rebuild_period"]) * args.steps,
-        "roofline": roofline, "e2e": e2e, "plain": plain,
-        "batched_over_plain": round(value / world / plain["value"], 2),
-        "plain3d": p3,
-        "batched3d": b3,
-        "disperse": disp,
-        "served": served,
-        "clocks": clock_info,
-    }
-    line["cpu_baseline"] = cpu_baseline(tissues, budget_s=args.cpu_budget)
-    return line
+        b.step(SIM_STEPS, DT)
+    it = max(3, args.steps)
+    s = timed(it, lambda: b.step(SIM_STEPS, DT))
+    return {"value": round(b.nverts * SIM_STEPS / s, 1), "unit": UNIT,
+            "ms_per_step": round(s * 1e3, 4), "sample": sample_desc(tissues),
+            "sim_steps_per_step": SIM_STEPS, "tuning": tuned}
 
 
-# ---------------------------------------------------------------------------
-# served mixed stream (continuous batching through dpm_serve_*)
-# ---------------------------------------------------------------------------
+def plain_c1(ctx, timed, geo, stages=125, relax=500, phi_start=0.6, dphi=0.002):
+    """The plain single-system path on the 2D jamming protocol: 1,024
+    bidisperse cells from packing fraction 0.6, compressed to 0.85 in steps
+    of 0.002 (dpm2d_set_packing_fraction on the device), 500 relaxation
+    steps per stage: 62,500 steps, timed whole."""
+    t = workload_c1(geo)
+    b, _ = make_batch(ctx, t)
+    tuned = b.autotune(DT, trial_blocks=2, use_cache=True)
+    b.step(relax, DT)  # the stage's graphs are captured outside the timed run
+    b.upload(t[0]["xy"])  # start over from the initial state
 
-SERVE_CHUNK = 256
-# (slots, cells per slot) of the 2D pools (NV <= 32) and of the 3D pools per
-# subdivision level; slot memory is small next to HBM, so the pools are sized
-# for concurrency
-POOLS_2D = [(48, 128), (32, 512), (24, 2048)]
-POOLS_3D = [(16, 128)]
+    def protocol():
+        for k in range(1, stages + 1):
+            b.set_packing_fraction(phi_start + k * dphi)
+            b.step(relax, DT)
+
+    secs, _ = timed.span(protocol)
+    d = b.diagnostics()
+    steps = stages * relax
+    return {"value": round(b.nverts * steps / secs, 1), "unit": UNIT,
+            "seconds": round(secs, 3), "sim_steps": steps,
+            "final": {"packing_fraction": round(float(d["packing_fraction"][0]), 5),
+                      "shape_index": round(float(d["shape_index"][0]), 5),
+                      "mean_energy": float(np.mean(d["energy"]))},
+            "workload": "1 tissue, 1024 cells x 32 vertices, bidisperse r0 1.0/1.4, "
+                        "calA0 ~ U[1.0,1.2], kb=0.01, ka=kl=kc=1, dt=0.005; packing fraction "
+                        f"{phi_start} -> {phi_start + stages * dphi:.3f} in steps of {dphi} "
+                        f"with {relax} relaxation steps each ({steps} steps, rescale on the "
+                        "device)",
+            "tuning": tuned}
 
 
-def served_requests(seed, nreq):
-    """70% 2D tissues drawn like the batched sweep with N ~ U{16..2048} and
-    NV in {16, 32}; 30% 3D monolayers with N ~ U{8..128} at subdivision 2 or
-    3; each runs U{1000..50000} steps."""
-    from opencl_dpm_gb300 import clDPM
-    rng = np.random.default_rng(seed)
-    reqs = []
-    for _ in range(nreq):
-        if rng.random() < 0.7:
-            n = int(rng.integers(16, 2049))
-            nv = int(rng.choice([16, 32]))
-            kb = float(10 ** rng.uniform(-3, -1))
-            calA = rng.uniform(1.0, 1.3, n)
-            phi = float(rng.uniform(0.6, 0.9))
-            t = build_tissue(clDPM, rng, n, np.full(n, nv), calA, np.ones(n), kb, phi)
-            t["dim"] = 2
-            t["verts"] = int(t["nv"].sum())
-        else:
-            n = int(rng.integers(8, 129))
-            t = build_monolayer(clDPM, rng, n, int(rng.choice([2, 3])))
-            t["verts"] = n * t["nv"]
-        t["steps"] = int(rng.integers(1000, 50001))
-        reqs.append(t)
-    return reqs
+def plain_c0(ctx, timed, geo, steps=10000):
+    """The reference's own CPU-runnable case: 16 cells x 32 vertices,
+    10,000 steps, timed whole."""
+    t = workload_c0(geo)
+    b, _ = make_batch(ctx, t)
+    tuned = b.autotune(DT, trial_blocks=2, use_cache=True)
+    b.upload(t[0]["xy"])
+    b.step(steps, DT)  # graphs captured outside the timed run
+    b.upload(t[0]["xy"])
+    secs, _ = timed.span(lambda: b.step(steps, DT))
+    return {"value": round(b.nverts * steps / secs, 1), "unit": UNIT,
+            "seconds": round(secs, 4), "sim_steps": steps,
+            "workload": "1 tissue, 16 cells x 32 vertices, calA0=1, ka=kl=kc=1, kb=0, "
+                        "packing fraction 0.6, uniform random centres, dt=0.005, 10,000 steps",
+            "tuning": tuned}
 
 
 def plain3d(ctx, timed, iters, steps=16):
     """The plain 3D monolayer: 256 icospheres at subdivision 3 (642 vertices,
-    1,280 faces), kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion range 0.1,
-    dt=0.002; `timed(iters, fn)` returns seconds for iters calls of fn."""
+    1,280 faces)."""
     from opencl_dpm_gb300 import clDPM
-    from opencl_dpm_gb300.abi import Batch3D
     t = build_monolayer(clDPM, np.random.default_rng(3), 256, 3)
-    b = Batch3D(ctx, [256], t["faces"], t["nv"])
-    b.set_cells(t["Kv"], t["Ka"], t["Ks"], t["v0"], t["a0"], t["l0"], t["Kb"], t["adh"])
-    b.set_tissues([t["L"]], 1.0, 1)
-    b.upload(t["xyz"])
+    b = make_batch3d(ctx, [t])
     for _ in range(3):
         b.step(steps, DT3)
     secs = timed(iters, lambda: b.step(steps, DT3))
-    return {"value": round(b.nverts * steps * iters / secs, 1), "unit": UNIT,
-            "ms_per_step": round(secs / iters * 1e3, 4), "sim_steps_per_step": steps,
+    return {"value": round(b.nverts * steps / secs, 1), "unit": UNIT,
+            "ms_per_step": round(secs * 1e3, 4), "sim_steps_per_step": steps,
             "workload": "1 monolayer, 256 cells x 642 vertices (icosphere subdivision 3), "
-                        "jittered hexagonal lattice on z=0, kv=1 ka=0.5 ks=0.1 kb=0.05, "
-                        "adhesion 0.1, dt=0.002"}
+                        "jittered hexagonal lattice on z=0, " + C2_NOTE}
 
 
 def batched3d(ctx, timed, iters, steps=16):
     """Many independent 3D monolayers in one batch: 48 tissues of N ~
-    U{8..64} cells at subdivision 3 (kv=1, ka=0.5, ks=0.1, kb=0.05, adhesion
-    0.1, dt=0.002), one launch per step for all of them."""
+    U{8..64} cells at subdivision 3, one launch per step for all of them."""
     from opencl_dpm_gb300 import clDPM
-    from opencl_dpm_gb300.abi import Batch3D
     rng = np.random.default_rng(5)
     ts = [build_monolayer(clDPM, rng, int(rng.integers(8, 65)), 3) for _ in range(48)]
-    cat = lambda k: np.concatenate([t[k] for t in ts])
-    b = Batch3D(ctx, [len(t["Kv"]) for t in ts], ts[0]["faces"], ts[0]["nv"])
-    b.set_cells(cat("Kv"), cat("Ka"), cat("Ks"), cat("v0"), cat("a0"), cat("l0"), cat("Kb"),
-                cat("adh"))
-    b.set_tissues([t["L"] for t in ts], 1.0, 1)
-    b.upload(cat("xyz"))
+    b = make_batch3d(ctx, ts)
     for _ in range(3):
         b.step(steps, DT3)
     secs = timed(iters, lambda: b.step(steps, DT3))
-    return {"value": round(b.nverts * steps * iters / secs, 1), "unit": UNIT,
-            "ms_per_step": round(secs / iters * 1e3, 4), "sim_steps_per_step": steps,
+    return {"value": round(b.nverts * steps / secs, 1), "unit": UNIT,
+            "ms_per_step": round(secs * 1e3, 4), "sim_steps_per_step": steps,
             "tissues": len(ts), "cells": int(sum(len(t["Kv"]) for t in ts)),
             "vertices": int(b.nverts),
             "workload": "48 monolayers, N ~ U{8..64} cells x 642 vertices (subdivision 3), "
-                        "kv=1 ka=0.5 ks=0.1 kb=0.05, adhesion 0.1, dt=0.002, one batch"}
+                        + C2_NOTE + ", one batch"}
 
 
-def disperse_leg(ctx, tissues):
+def steady_state_leg(ctx, timed, geo, total=20000):
+    """The sweep's full 20,000-step run from its initial lattice, in calls of
+    32 steps timed one by one (no L2 flush: a continuous run): rate over the
+    first 640 steps, around steps 2,000 and 10,000, the last 640, and the
+    whole run."""
+    tissues = workload_batched(geo)
+    b, _ = make_batch(ctx, tissues)
+    b.autotune(DT, trial_blocks=2, use_cache=True)
+    b.step(SIM_STEPS, DT)  # graphs captured outside the timed run
+    b.upload(np.concatenate([t["xy"] for t in tissues]))
+    import torch
+    calls = total // SIM_STEPS
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(calls + 1)]
+    with torch.cuda.stream(timed.stream):
+        ev[0].record(timed.stream)
+        for i in range(calls):
+            b.step(SIM_STEPS, DT)
+            ev[i + 1].record(timed.stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    ms = np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(calls)])
+    rate = lambda a, z: round(b.nverts * SIM_STEPS * (z - a) / (ms[a:z].sum() / 1e3), 1)
+    w = 20
+    return {"unit": UNIT, "sim_steps": calls * SIM_STEPS,
+            "steps_0_640": rate(0, w), "steps_2000_2640": rate(62, 62 + w),
+            "steps_10000_10640": rate(312, 312 + w), "last_640": rate(calls - w, calls),
+            "whole_run": rate(0, calls), "rebuilds_fallback": b.stats()[1]}
+
+
+def disperse_leg(ctx, tissues, geo):
     """Setup cost: the reference's dispersion of cell centres (bit-exact on
     the device, dpm_disperse) for every tissue of the batched workload in one
     launch, and for the 1,024-cell plain tissue; the host loop on a few
@@ -510,7 +707,7 @@ def disperse_leg(ctx, tissues):
         return time.perf_counter() - t0, it
 
     batch_s, batch_it = run(tissues, 1)
-    plain = workload_plain()
+    plain = workload_c1(geo)
     plain_s, plain_it = run(plain, 7)
     # host loop on the four tissues nearest 64 cells, and the device on the same
     near = sorted(range(len(tissues)), key=lambda k: abs(len(tissues[k]["nv"]) - 64))[:4]
@@ -529,6 +726,45 @@ def disperse_leg(ctx, tissues):
             "note": "bit-exact with the reference's host loop; one thread block per tissue"}
 
 
+# ---------------------------------------------------------------------------
+# served mixed stream (continuous batching through dpm_serve_*)
+# ---------------------------------------------------------------------------
+
+SERVE_CHUNK = 256
+# (slots, cells per slot) of the 2D pools (NV <= 32) and of the 3D pools per
+# subdivision level; slot memory is small next to HBM, so the pools are sized
+# for concurrency
+POOLS_2D = [(48, 128), (32, 512), (24, 2048)]
+POOLS_3D = [(16, 128)]
+
+
+def served_requests(seed, nreq):
+    """70% 2D tissues drawn like the batched sweep with N ~ U{16..2048} and
+    NV in {16, 32}; 30% 3D monolayers with N ~ U{8..128} at subdivision 2 or
+    3; each runs U{1000..50000} steps."""
+    from opencl_dpm_gb300 import clDPM
+    geo = ProductGeometry()
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(nreq):
+        if rng.random() < 0.7:
+            n = int(rng.integers(16, 2049))
+            nv = int(rng.choice([16, 32]))
+            kb = float(10 ** rng.uniform(-3, -1))
+            calA = rng.uniform(1.0, 1.3, n)
+            phi = float(rng.uniform(0.6, 0.9))
+            t = build_tissue(geo, rng, n, np.full(n, nv), calA, np.ones(n), kb, phi)
+            t["dim"] = 2
+            t["verts"] = int(t["nv"].sum())
+        else:
+            n = int(rng.integers(8, 129))
+            t = build_monolayer(clDPM, rng, n, int(rng.choice([2, 3])))
+            t["verts"] = n * t["nv"]
+        t["steps"] = int(rng.integers(1000, 50001))
+        reqs.append(t)
+    return reqs
+
+
 def make_server(ctx):
     from opencl_dpm_gb300 import clDPM
     from opencl_dpm_gb300.abi import Server
@@ -536,7 +772,7 @@ def make_server(ctx):
     for slots, cells in POOLS_2D:
         srv.add_pool2d(slots, cells, 32, DT)
     for level in (2, 3):
-        proto = clDPM.Cell3D([0.0, 0.0, 0.0], 1.05, 1.0, level)
+        proto = clDPM.Cell3D([0.0, 0.0, 0.0], 1.0, 1.0, level)
         faces = np.asarray(proto.GetFaces(), np.uint32)
         for slots, cells in POOLS_3D:
             srv.add_pool3d(slots, cells, faces, int(proto.NV), DT3)
@@ -568,7 +804,7 @@ def served_capacity(ctx, seed, nreq=32, steps=2048):
     return vs / secs
 
 
-def run_served(ctx, nreq, seed=77):
+def run_served(ctx, nreq, plain2d, plain3d, seed=77):
     """Seeded Poisson arrivals at 80% of the server's measured capacity for
     this request mix; latency = completion - arrival (host clock)."""
     reqs = served_requests(seed, nreq)
@@ -609,9 +845,11 @@ def run_served(ctx, nreq, seed=77):
     lat = done_at - arrival
     vs, _ = srv.stats()
     srv.close()
-    n2 = sum(1 for t in reqs if t["dim"] == 2)
     dims = np.array([t["dim"] for t in reqs])
+    n2 = int(np.sum(dims == 2))
     slow = int(np.argmax(lat))
+    vs2 = float(sum(t["verts"] * t["steps"] for t in reqs if t["dim"] == 2))
+    vs3 = float(sum(t["verts"] * t["steps"] for t in reqs if t["dim"] == 3))
 
     def pct(x):
         return {"p50": round(float(np.percentile(x, 50)), 4),
@@ -619,6 +857,12 @@ def run_served(ctx, nreq, seed=77):
 
     return {
         "value": round(vs / makespan, 1), "unit": UNIT,
+        "by_dim": {"2d": {"value": round(vs2 / makespan, 1),
+                          "over_plain_2d": round(vs2 / makespan / plain2d, 3)},
+                   "3d": {"value": round(vs3 / makespan, 1),
+                          "over_plain_3d": round(vs3 / makespan / plain3d, 3)},
+                   "note": "each dimension's vertex-steps over the whole makespan (2D and 3D "
+                           "requests share the GPU), against its own plain path"},
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 4),
                       "p99": round(float(np.percentile(lat, 99)), 4),
                       "max": round(float(lat.max()), 4),
@@ -637,13 +881,12 @@ def run_served(ctx, nreq, seed=77):
                   "bytes": pool_bytes, "chunk_steps": SERVE_CHUNK},
         "workload": "seeded Poisson arrivals; 70% 2D (N~U{16..2048}, NV in {16,32}, params as "
                     "the batched sweep, dt=0.005), 30% 3D monolayers (N~U{8..128}, subdivision "
-                    "2 or 3, kv=1 ka=0.5 ks=0.1 kb=0.05 adhesion 0.1, dt=0.002); "
-                    "steps~U{1000..50000}",
+                    "2 or 3, " + C2_NOTE + "); steps~U{1000..50000}",
     }
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline and the reference arm (the oracle; test/baseline use only)
+# CPU baselines and the reference arm (the oracle; baseline use only)
 # ---------------------------------------------------------------------------
 
 def oracle_states(tissues):
@@ -653,56 +896,114 @@ def oracle_states(tissues):
             for t in tissues]
 
 
-def cpu_sample(tissues, every=16):
-    return tissues[::every]
-
-
-def cpu_baseline(tissues, budget_s=10.0, steps=None):
+def timed_oracle_2d(states, steps_per_round, threads, budget_s, max_rounds=None):
+    """Rounds of `steps_per_round` oracle steps over every state until the
+    budget is spent (at least one round); returns (vertex-steps/s, steps)."""
     from oracle.oracle import Port
     P = Port()
-    sample = oracle_states(cpu_sample(tissues))
-    cores = os.cpu_count() or 1
-    verts = sum(int(s.nv.sum()) for s in sample)
+    verts = sum(int(s.nv.sum()) for s in states)
     t0 = time.perf_counter()
     done = 0
     while True:
-        for s in sample:
-            P.run2d(s, 1, DT, nthreads=cores)
-        done += 1
+        for s in states:
+            P.run2d(s, steps_per_round, DT, nthreads=threads)
+        done += steps_per_round
         el = time.perf_counter() - t0
-        if (steps is not None and done >= steps) or (steps is None and el >= budget_s):
+        if el >= budget_s or (max_rounds is not None and done >= max_rounds * steps_per_round):
             break
-    return {"value": round(verts * done / el, 1), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{len(sample)} of {len(tissues)} tissues (every 16th, {verts} vertices), "
-                      f"{done} steps, all-pairs reference algorithm, OpenMP over cells"}
+    return verts * done / el, done
+
+
+def cpu_baseline(tissues, budget_s=10.0):
+    """The sweep's sample (every 16th tissue) on all host cores."""
+    cores = os.cpu_count() or 1
+    rate, done = timed_oracle_2d(oracle_states(sweep_sample(tissues)), 1, cores, budget_s)
+    return {"value": round(rate, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{sample_desc(tissues)}, {done} steps, all-pairs reference algorithm, "
+                      "OpenMP over cells"}
+
+
+def cpu_baselines_plain(geo, budget_s=10.0):
+    """The plain configurations on the host cores, single-thread and
+    all-core (the oracle restatement: the reference's all-pairs algorithm)."""
+    from oracle.oracle import Port, Tissue3DState
+    from opencl_dpm_gb300 import clDPM
+    cores = os.cpu_count() or 1
+    out = {"kind": "port", "cores_all": cores}
+    # 16 cells: every one of the 10,000 steps on all cores; a share single-thread
+    c0 = oracle_states(workload_c0(geo))
+    r_all, n_all = timed_oracle_2d([c0[0].copy()], 10000, cores, 0.0, max_rounds=1)
+    r_one, n_one = timed_oracle_2d([c0[0].copy()], 500, 1, budget_s / 4)
+    out["c0"] = {"all_cores": round(r_all, 1), "all_cores_steps": n_all,
+                 "single_thread": round(r_one, 1), "single_thread_steps": n_one,
+                 "sample": "16 cells x 32 vertices (the whole workload)"}
+    # 1,024 cells at packing fraction 0.6 (the protocol's first stage)
+    c1 = oracle_states(workload_c1(geo))
+    r_all, n_all = timed_oracle_2d([c1[0].copy()], 1, cores, budget_s / 4)
+    r_one, n_one = timed_oracle_2d([c1[0].copy()], 1, 1, budget_s / 8, max_rounds=1)
+    out["c1"] = {"all_cores": round(r_all, 1), "all_cores_steps": n_all,
+                 "single_thread": round(r_one, 1), "single_thread_steps": n_one,
+                 "sample": "1024 cells x 32 vertices at packing fraction 0.6"}
+    # 3D monolayer: all-pairs winding numbers at subdivision 3; 32 cells on
+    # all cores, 8 single-thread (the all-pairs sum grows as cells squared)
+    P = Port()
+    res = {}
+    for name, ncell, thr in (("all_cores", 32, cores), ("single_thread", 8, 1)):
+        t = build_monolayer(clDPM, np.random.default_rng(3), ncell, 3)
+        s = Tissue3DState(nv=t["nv"], faces=t["faces"], xyz=t["xyz"].copy(), Kv=t["Kv"],
+                          Ka=t["Ka"], Ks=t["Ks"], v0=t["v0"], a0=t["a0"], l0=t["l0"],
+                          L=float(t["L"]), Kre=1.0, pbc=1, Kb=t["Kb"], adh=t["adh"])
+        t0 = time.perf_counter()
+        P.run3d(s, 1, DT3, nthreads=thr)
+        res[name] = round(s.xyz.shape[0] / (time.perf_counter() - t0), 1)
+        res[name + "_cells"] = ncell
+    out["c2"] = dict(res, steps=1,
+                     sample="monolayers of 32 (all cores) and 8 (one thread) cells x 642 "
+                            "vertices (subdivision 3), one step; the oracle's winding sum runs "
+                            "over all cell pairs, so the 256-cell rate is ~8x below the 32-cell "
+                            "one")
+    return out
 
 
 def run_reference(args):
-    tissues = workload_batched(seed=1000)
+    """The reference arm: the oracle (the reference's algorithm restated in
+    C; the reference's own OpenCL path cannot run on this machine, and its
+    CPU build needs its source tree) on the host cores, over the sweep's
+    32-tissue sample, 32 simulation steps per benchmark step.  Its inputs come
+    from the oracle's own geometry: nothing of the product is loaded."""
+    tissues = workload_batched(OracleGeometry())
+    sample = oracle_states(sweep_sample(tissues))
     from oracle.oracle import Port
     P = Port()
-    sample = oracle_states(cpu_sample(tissues))
     cores = os.cpu_count() or 1
     verts = sum(int(s.nv.sum()) for s in sample)
-    for _ in range(args.warmup):
+
+    def one():
         for s in sample:
-            P.run2d(s, 1, DT, nthreads=cores)
+            P.run2d(s, SIM_STEPS, DT, nthreads=cores)
+
+    for _ in range(args.warmup):
+        one()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for s in sample:
-            P.run2d(s, 1, DT, nthreads=cores)
+        one()
     secs = time.perf_counter() - t0
-    value = verts * args.steps / secs
-    desc = (f"{len(sample)} of {len(tissues)} tissues (every 16th, {verts} vertices), "
-            f"one simulation step per benchmark step, all-pairs reference algorithm")
+    value = verts * SIM_STEPS * args.steps / secs
+    desc = (f"{sample_desc(tissues)}, {SIM_STEPS} simulation steps per benchmark step, "
+            "all-pairs reference algorithm, OpenMP over cells")
+    ncells = sum(len(t["nv"]) for t in tissues)
+    nverts = sum(int(t["nv"].sum()) for t in tissues)
     return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded tissues)",
-            "config": {"workload": WORKLOAD_SWEEP, "sample": desc},
+            "data": "synthetic (seeded tissues; see config)",
+            "config": sweep_config(len(tissues), ncells, nverts),
             "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores,
-                             "kind": "port", "sample": desc},
+                             "threads": cores, "kind": "port",
+                             "oracle": "oracle/dpm_oracle.c (the oracle restatement; "
+                                       "oracle/_ref needs the reference tree)",
+                             "sample": desc},
             "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 

@@ -36,7 +36,7 @@ def tissue_state2d(t, xy):
 
 def test_sweep_2d_full_size(ctx):
     import bench
-    tissues = bench.workload_batched(seed=1000)
+    tissues = bench.workload_batched(bench.ProductGeometry(), seed=1000)
     nsteps = 64
     runs = []
     for _ in range(2):

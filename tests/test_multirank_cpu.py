@@ -29,7 +29,7 @@ def _rank(rank, world, port, out):
                             world_size=world)
     try:
         # each rank's shard is seeded by its rank, as in bench.run_ours
-        shard = bench.workload_batched(seed=1000 + rank, ntissues=3)
+        shard = bench.workload_batched(bench.OracleGeometry(), seed=1000 + rank, ntissues=3)
         verts = sum(int(t["nv"].sum()) for t in shard)
         secs, units = bench.reduce_over_ranks(1.0 + rank, float(verts), world, "cpu")
         out[rank] = (secs, units, verts, float(shard[0]["xy"][0, 0]))
