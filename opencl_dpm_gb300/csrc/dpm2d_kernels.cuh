@@ -25,6 +25,9 @@ struct Step2DArgs {
   int all_forces;  // 1: force_out/flags_out take every cell's values; 0: only
                    // those of tissues whose step budget ends at this step
   int *sched;      // two zeroed counters for the dynamic schedule, or nullptr
+  const int *order; // the launch's cells: order[0..ncells), or nullptr for
+                    // cells 0..ncells-1 (a batch of mixed ring sizes launches
+                    // one kernel per vertex-slot class over its own cells)
 };
 
 struct Rebuild2DArgs {

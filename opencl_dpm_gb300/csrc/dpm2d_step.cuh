@@ -397,8 +397,9 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
   __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
   __shared__ unsigned char sh_f[W][M];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * W + w;
-  if (c >= a.ncells) return;
+  const int i = blockIdx.x * W + w;
+  if (i >= a.ncells) return;
+  const int c = a.order ? a.order[i] : i;
   step_cell<S, ATT>(a, c, lane, sh_x[w], sh_y[w], sh_nx[w], sh_ny[w], sh_f[w]);
 }
 
@@ -415,10 +416,11 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
   __shared__ unsigned char sh_f[W][M];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
-    int c = 0;
-    if (lane == 0) c = atomicAdd(a.sched, 1);
-    c = __shfl_sync(kFull, c, 0);
-    if (c >= a.ncells) break;
+    int i = 0;
+    if (lane == 0) i = atomicAdd(a.sched, 1);
+    i = __shfl_sync(kFull, i, 0);
+    if (i >= a.ncells) break;
+    const int c = a.order ? a.order[i] : i;
     step_cell<S, ATT>(a, c, lane, sh_x[w], sh_y[w], sh_nx[w], sh_ny[w], sh_f[w]);
     __syncwarp();
   }

@@ -90,8 +90,20 @@ struct dpm2d_batch {
   Geom2D *d_geom[2] = {nullptr, nullptr};
   Geom2D *d_geom0 = nullptr;
   int *d_nn = nullptr, *d_nbr = nullptr, *d_stale = nullptr, *d_err = nullptr;
-  int *d_sched = nullptr; // dynamic-schedule counters of the step kernel
+  int *d_sched = nullptr; // dynamic-schedule counters of the step kernel (per class)
   float *d_phi = nullptr; // per-tissue packing fractions of a rescale
+
+  // Vertex-slot classes (rings of at most 32, 64, 128, 256 vertices, one
+  // warp lane holding 1, 2, 4, 8 of them).  A batch whose cells fall into
+  // more than one class launches one step kernel per class over its own
+  // cells (d_order[class_begin[k] .. class_begin[k+1])), side by side on
+  // two streams (a fork and join inside the captured graph), so that every
+  // cell runs the code compiled for its ring size.
+  int nclass = 1;
+  int class_begin[5] = {0, 0, 0, 0, 0};
+  int *d_order = nullptr;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   uint32_t *d_keys = nullptr, *d_vals = nullptr, *d_keys_alt = nullptr, *d_vals_alt = nullptr;
   uint32_t *d_sort_scratch = nullptr;
   int cur = 0;
@@ -120,6 +132,12 @@ struct dpm2d_batch {
       cudaStreamSynchronize(stream);
       cudaStreamDestroy(stream);
     }
+    if (aux) {
+      cudaStreamSynchronize(aux);
+      cudaStreamDestroy(aux);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
   }
   void clear_graphs() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -195,13 +213,37 @@ struct dpm2d_batch {
     return a;
   }
 
+  // One step of every cell: a single launch, or one launch per vertex-slot
+  // class, the largest rings first on the auxiliary stream and the smallest
+  // on `s`, joined back into `s`.  The classes write disjoint cells and read
+  // only the step's inputs, so their order does not matter.
+  cudaError_t launch_step(const Step2DArgs &a0, cudaStream_t s) {
+    if (serving || nclass <= 1) return launch_step2d(a0, maxnv, warps, variant(), s);
+    cudaError_t e = cudaEventRecord(ev_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev_fork, 0);
+    int first = 0;
+    while (class_begin[first + 1] == class_begin[first]) ++first;
+    for (int k = 3; k >= first && e == cudaSuccess; --k) {
+      const int n = class_begin[k + 1] - class_begin[k];
+      if (n == 0) continue;
+      Step2DArgs a = a0;
+      a.order = d_order + class_begin[k];
+      a.ncells = n;
+      a.sched = d_sched + 2 * k;
+      e = launch_step2d(a, 32 << k, warps, variant(), k == first ? s : aux);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev_join, aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
+    return e;
+  }
+
   // Enqueue a block: rebuild, then `len` steps starting from buffer `from`.
   cudaError_t enqueue_block(int len, int from, float dt, bool last, cudaStream_t s) {
     cudaError_t e = enqueue_rebuild(from, len, s);
     if (e != cudaSuccess) return e;
     int f = from;
     for (int i = 0; i < len; ++i) {
-      e = launch_step2d(step_args(f, dt, last && i == len - 1, i), maxnv, warps, variant(), s);
+      e = launch_step(step_args(f, dt, last && i == len - 1, i), s);
       if (e != cudaSuccess) return e;
       f = 1 - f;
     }
@@ -326,6 +368,18 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     }
     if (off > (1L << 31) - 1) return fail(DPM_ECAPACITY, "too many vertices");
     b->nverts = off;
+    // vertex-slot classes and the cells of each, in cell order
+    auto slot_class = [](unsigned v) { return v <= 32 ? 0 : v <= 64 ? 1 : v <= 128 ? 2 : 3; };
+    int cnt[4] = {0, 0, 0, 0};
+    for (long c = 0; c < total_cells; ++c) ++cnt[slot_class(nv[c])];
+    b->nclass = (cnt[0] > 0) + (cnt[1] > 0) + (cnt[2] > 0) + (cnt[3] > 0);
+    std::vector<int> order;
+    if (b->nclass > 1) {
+      for (int k = 0; k < 4; ++k) b->class_begin[k + 1] = b->class_begin[k] + cnt[k];
+      order.resize(total_cells);
+      int fill[4] = {b->class_begin[0], b->class_begin[1], b->class_begin[2], b->class_begin[3]};
+      for (long c = 0; c < total_cells; ++c) order[fill[slot_class(nv[c])]++] = (int)c;
+    }
     b->h_cells.resize(total_cells);
     b->h_Ka.assign(total_cells, 0.0f);
     b->h_Kl.assign(total_cells, 0.0f);
@@ -356,7 +410,8 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     e = A.reserve(sizeof(Cell2D) * N + sizeof(Tissue2D) * ntissues + 3 * sizeof(float2) * V +
                   V + 3 * sizeof(Geom2D) * N + sizeof(int) * (N + N * kMaxNB2D) +
-                  sizeof(int) * (ntissues + 1) + sizeof(float) * ntissues +
+                  sizeof(int) * (ntissues + 1) + sizeof(float) * ntissues + sizeof(int) * 8 +
+                  (b->nclass > 1 ? sizeof(int) * N : 0) +
                   4 * sizeof(uint32_t) * N +
                   radix_sort_scratch_bytes((int)N) + 64 * 256);
     if (e != cudaSuccess) return cuda_fail(e, "device allocation");
@@ -373,8 +428,9 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     b->d_nbr = A.take<int>(N * kMaxNB2D);
     b->d_stale = A.take<int>(ntissues);
     b->d_err = A.take<int>(1);
-    b->d_sched = A.take<int>(2);
+    b->d_sched = A.take<int>(8);
     b->d_phi = A.take<float>(ntissues);
+    if (b->nclass > 1) b->d_order = A.take<int>(N);
     b->d_keys = A.take<uint32_t>(N);
     b->d_vals = A.take<uint32_t>(N);
     b->d_keys_alt = A.take<uint32_t>(N);
@@ -383,6 +439,15 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     if (!A.ok()) return fail(DPM_ECAPACITY, "device arena exhausted");
     e = cudaMemsetAsync(A.base(), 0, A.used(), ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    if (b->nclass > 1) {
+      e = cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * N, cudaMemcpyHostToDevice,
+                          ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "vertex-slot classes");
+    }
     *out = b.release();
     ctx_retain(ctx);
     return DPM_OK;
@@ -551,8 +616,7 @@ int dpm2d_step_kernel(dpm2d_batch *b, float dt) {
   if (int r = check_batch(b)) return r;
   if (!b->uploaded || !b->tissues_set) return fail(DPM_ESTATE, "upload before stepping");
   cudaSetDevice(b->ctx->device);
-  DPM_CUDA_TRY(launch_step2d(b->step_args(b->cur, dt, true, 0), b->maxnv, b->warps, b->variant(),
-                             b->stream));
+  DPM_CUDA_TRY(b->launch_step(b->step_args(b->cur, dt, true, 0), b->stream));
   b->cur = 1 - b->cur;
   return DPM_OK;
 }
