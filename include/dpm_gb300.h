@@ -206,11 +206,20 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache,
  *   - ncells <= DPM_NOALLOC_MAX_CELLS and total vertices <=
  *     DPM_NOALLOC_MAX_VERTICES, 3..256 vertices per cell; larger inputs are
  *     rejected with DPM_ECAPACITY;
- *   - every call shares that array: calls that overlap on the GPU (from two
- *     threads, or on unordered streams) race; calls on one stream are safe;
- *   - the first call on a device looks up the array's device address once.
- * Work is enqueued on `stream` (a cudaStream_t; NULL for the default stream)
- * and the call returns after it completes. */
+ *   - every call shares that array, and its contents are not valid between
+ *     calls.  Calls are serialized by a process-wide lock (calls on
+ *     different devices too), and each returns only after its work is done,
+ *     so calls from several host threads never overlap inside the library;
+ *   - the first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) once and keeps it for the life of the process:
+ *     do not reset the device (cudaDeviceReset) between calls, and call from
+ *     the device's primary context;
+ *   - nsteps == 0 does no device work (xy_dev and F_dev are left as they
+ *     are).
+ * Work is enqueued on `stream` (a cudaStream_t) and the call blocks until
+ * that stream has drained.  NULL means the legacy default stream, which also
+ * waits for every other blocking stream on the device: a caller that must
+ * not synchronize the whole device passes its own non-blocking stream. */
 #define DPM_NOALLOC_MAX_CELLS 2048
 #define DPM_NOALLOC_MAX_VERTICES 65536
 int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *Ka,

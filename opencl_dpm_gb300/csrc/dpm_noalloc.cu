@@ -13,10 +13,13 @@
 // that loads the library holds until the process exits.
 //
 // Limits: at most DPM_NOALLOC_MAX_CELLS cells and DPM_NOALLOC_MAX_VERTICES
-// vertices (3..256 per cell), one tissue.  All calls share the array; calls
-// that overlap on the GPU (from two threads, or on two streams without
-// ordering) race on it.  The first call on a device looks up the array's
-// device address (cudaGetSymbolAddress) once for that device.
+// vertices (3..256 per cell), one tissue.  All calls share the array and
+// its contents are not valid between calls; a process-wide lock serializes
+// the calls (on every device) and each returns after its stream drains, so
+// calls never overlap inside the library.  The first call on a device looks
+// up the array's device address (cudaGetSymbolAddress) once for that device
+// and keeps it for the life of the process (the primary context must not be
+// reset between calls).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -115,6 +118,7 @@ extern "C" int dpm2d_step_noalloc(int ncells, const unsigned *nv, const float *K
   if (total > kMaxVerts)
     return fail(DPM_ECAPACITY,
                 "dpm2d_step_noalloc: more than DPM_NOALLOC_MAX_VERTICES (65536) vertices");
+  if (nsteps == 0) return DPM_OK;  // nothing to step: no device work
 
   std::lock_guard<std::mutex> lock(g_mu);
   int device = 0;

@@ -33,12 +33,12 @@ def noalloc_fn():
     return fn
 
 
-def call_noalloc(fn, s, xy_dev, F_dev, nsteps):
+def call_noalloc(fn, s, xy_dev, F_dev, nsteps, stream=None):
     arrs = [np.ascontiguousarray(getattr(s, k), np.float32)
             for k in ("Ka", "Kl", "Kb", "a0", "l0", "r0")]
     nv = np.ascontiguousarray(s.nv, np.uint32)
     return fn(len(nv), nv.ctypes.data_as(_u), *[a.ctypes.data_as(_f) for a in arrs], s.L, s.Kre,
-              s.Kat, int(s.pbc), xy_dev, F_dev, nsteps, DT, None)
+              s.Kat, int(s.pbc), xy_dev, F_dev, nsteps, DT, stream)
 
 
 def batch_run(ctx, s, nsteps):
@@ -82,3 +82,32 @@ def test_noalloc_rejects_oversize():
             dummy.ctypes.data, None, 1, DT, None)
     assert rc == 3  # DPM_ECAPACITY
     assert b"2048" in load().dpm_last_error()
+
+
+@pytest.mark.gpu
+def test_noalloc_on_own_stream_against_oracle():
+    """A caller that must not synchronize the whole device passes its own
+    non-blocking stream (here a torch stream's handle); the result also
+    matches the oracle directly.  nsteps == 0 leaves the buffers alone."""
+    import torch
+    from cases import port
+    fn = noalloc_fn()
+    s = make_tissue2d(30, 32, phi=0.85, Kb=0.02, seed=33)
+    st = torch.cuda.Stream(device=0)
+    xy = torch.from_numpy(s.xy.copy()).to("cuda:0")
+    F = torch.full_like(xy, 7.0)
+    torch.cuda.synchronize()
+    assert call_noalloc(fn, s, xy.data_ptr(), F.data_ptr(), 0, st.cuda_stream) == 0
+    assert np.array_equal(xy.cpu().numpy(), s.xy) and bool(torch.all(F == 7.0))
+    assert call_noalloc(fn, s, xy.data_ptr(), F.data_ptr(), 25, st.cuda_stream) == 0
+    r = s.copy()
+    rF, _ = port().run2d(r, 25, DT)
+    x_out = xy.cpu().numpy()
+    assert float(np.max(np.abs(x_out - r.xy) / np.maximum(np.abs(r.xy), 1.0))) <= X_TOL
+    # forces of one step from the device's positions, against the oracle
+    s1 = s.copy()
+    s1.xy = x_out.copy()
+    assert call_noalloc(fn, s1, xy.data_ptr(), F.data_ptr(), 1, st.cuda_stream) == 0
+    r1 = s1.copy()
+    rF1, _ = port().run2d(r1, 1, DT)
+    assert rel_norm_err(F.cpu().numpy(), rF1) <= F_TOL
