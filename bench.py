@@ -431,7 +431,9 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     clocks = ClockSampler(local_rank)
     clocks.start()
+    torch.cuda.nvtx.range_push("headline")
     secs = timed(args.steps, lambda: b.step(SIM_STEPS, DT)) * args.steps
+    torch.cuda.nvtx.range_pop()
     clock_info = clocks.stop()
     torch.cuda.synchronize()
     secs, units = reduce_over_ranks(secs, float(V) * SIM_STEPS * args.steps, world,
@@ -492,13 +494,19 @@ def sweep_config(ntissues, ncells, nverts):
 
 def step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info):
     """HBM and issue rooflines of the fused step kernel (k2d_step)."""
-    # one launch at a time after an L2 flush (cold), and the kernel's share
-    # of the graph: the graph's time per simulation step less the rebuild
+    # one launch at a time after an L2 flush (cold), and launches as they run
+    # inside a graph: one rebuild period of step launches queued back to back
+    # after a fresh neighbour-list rebuild, warm, timed together
     nk = 20
     kern = timed(nk, lambda: b.step_kernel(DT))
-    rebuild_s, _ = timed.span(b.rebuild_now)
     period = tuned["rebuild_period"]
-    in_graph = (ms_per_step / 1e3 - rebuild_s * SIM_STEPS / period) / SIM_STEPS
+
+    def period_of_steps():
+        for _ in range(period):
+            b.step_kernel(DT)
+
+    b.rebuild_now()
+    in_graph = timed(1, period_of_steps, flush=False) / period
     bytes_per_launch = 16.0 * V + 28.0 * N
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_per_launch / in_graph / 1e9
@@ -515,10 +523,12 @@ def step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info):
                            str(prof["build"]) + ")"}
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS)",
-            "kernel": "k2d_step", "in_graph_us": round(in_graph * 1e6, 2),
+            "kernel": "k2d_step (one launch per vertex-slot class, together)",
+            "in_graph_us": round(in_graph * 1e6, 2),
+            "in_graph_how": "a rebuild period of step launches queued back to back after a "
+                            "rebuild, warm (the graph's launches without the graph)",
             "cold_single_launch_us": round(kern * 1e6, 2),
             "cold_frac": round(bytes_per_launch / kern / 1e9 / peak, 4),
-            "rebuild_us": round(rebuild_s * 1e6, 2),
             "bytes_per_launch": int(bytes_per_launch),
             "traffic": None if prof["traffic"] is None else int(prof["traffic"]),
             "traffic_source": "profiles/k2d_step_batched512.md (ncu dram__bytes_read.sum + "
@@ -590,11 +600,14 @@ def plain_c1(ctx, timed, geo, stages=125, relax=500, phi_start=0.6, dphi=0.002):
 
     secs, _ = timed.span(protocol)
     d = b.diagnostics()
+    si = d["perimeter"] / np.sqrt(4.0 * np.pi * d["area"])
     steps = stages * relax
     return {"value": round(b.nverts * steps / secs, 1), "unit": UNIT,
             "seconds": round(secs, 3), "sim_steps": steps,
             "final": {"packing_fraction": round(float(d["packing_fraction"][0]), 5),
-                      "shape_index": round(float(d["shape_index"][0]), 5),
+                      "shape_index_median": round(float(np.median(si)), 5),
+                      "shape_index_mean": round(float(d["shape_index"][0]), 5),
+                      "cells_below_half_a0": int(np.sum(d["area"] < 0.5 * t[0]["a0"])),
                       "mean_energy": float(np.mean(d["energy"]))},
             "workload": "1 tissue, 1024 cells x 32 vertices, bidisperse r0 1.0/1.4, "
                         "calA0 ~ U[1.0,1.2], kb=0.01, ka=kl=kc=1, dt=0.005; packing fraction "
@@ -1008,6 +1021,40 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
 
 
+def run_profile(kind):
+    """A profiling target: the workload is set up and warmed as in the
+    benchmark, then the launches to capture run inside the NVTX range
+    "profile" (ncu --nvtx --nvtx-include "profile/"): for "2d" one fused step
+    of the batched sweep (one launch per vertex-slot class) after a fresh
+    neighbour-list rebuild; for "3d" one step of the 256-cell monolayer."""
+    import torch
+    from opencl_dpm_gb300.abi import Context
+    ctx = Context(0)
+    if kind == "2d":
+        tissues = workload_batched(ProductGeometry())
+        b, _ = make_batch(ctx, tissues)
+        b.autotune(DT, trial_blocks=2, use_cache=True)
+        for _ in range(5):
+            b.step(SIM_STEPS, DT)
+        b.rebuild_now()
+        torch.cuda.nvtx.range_push("profile")
+        b.step_kernel(DT)
+        ctx.synchronize()
+        torch.cuda.nvtx.range_pop()
+    else:
+        from opencl_dpm_gb300 import clDPM
+        t = build_monolayer(clDPM, np.random.default_rng(3), 256, 3)
+        b = make_batch3d(ctx, [t])
+        for _ in range(3):
+            b.step(16, DT3)
+        ctx.synchronize()
+        torch.cuda.nvtx.range_push("profile")
+        b.step(1, DT3)
+        ctx.synchronize()
+        torch.cuda.nvtx.range_pop()
+    print(json.dumps({"profile": kind, "ok": True}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1017,7 +1064,12 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests in the served mixed stream (0 skips it)")
+    ap.add_argument("--profile", choices=["2d", "3d"], default=None,
+                    help="run only a profiling target (see run_profile)")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args.profile)
+        return 0
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
