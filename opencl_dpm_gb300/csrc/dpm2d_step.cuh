@@ -415,14 +415,11 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
   __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
   __shared__ unsigned char sh_f[W][M];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int nxt = 0;
-  if (lane == 0) nxt = atomicAdd(a.sched, 1);
   for (;;) {
-    const int i = __shfl_sync(kFull, nxt, 0);
+    int i = 0;
+    if (lane == 0) i = atomicAdd(a.sched, 1);
+    i = __shfl_sync(kFull, i, 0);
     if (i >= a.ncells) break;
-    // the next cell's index is fetched while this one is stepped: every
-    // warp of the grid draws from one counter, and its latency hides here
-    if (lane == 0) nxt = atomicAdd(a.sched, 1);
     const int c = a.order ? a.order[i] : i;
     step_cell<S, ATT>(a, c, lane, sh_x[w], sh_y[w], sh_nx[w], sh_ny[w], sh_f[w]);
     __syncwarp();

@@ -94,11 +94,12 @@ struct dpm2d_batch {
   float *d_phi = nullptr; // per-tissue packing fractions of a rescale
 
   // Vertex-slot classes (rings of at most 32, 64, 128, 256 vertices, one
-  // warp lane holding 1, 2, 4, 8 of them).  A batch whose cells fall into
-  // more than one class launches one step kernel per class over its own
-  // cells (d_order[class_begin[k] .. class_begin[k+1])), side by side on
-  // two streams (a fork and join inside the captured graph), so that every
-  // cell runs the code compiled for its ring size.
+  // warp lane holding 1, 2, 4, 8 of them).  A cell's class is that of its
+  // tissue's largest ring.  A batch whose tissues fall into more than one
+  // class launches one step kernel per class over its own cells
+  // (d_order[class_begin[k] .. class_begin[k+1])), side by side on two
+  // streams (a fork and join inside the captured graph), so that every
+  // tissue runs the code compiled for its ring sizes.
   int nclass = 1;
   int class_begin[5] = {0, 0, 0, 0, 0};
   int *d_order = nullptr;
@@ -214,9 +215,10 @@ struct dpm2d_batch {
   }
 
   // One step of every cell: a single launch, or one launch per vertex-slot
-  // class, the largest rings first on the auxiliary stream and the smallest
-  // on `s`, joined back into `s`.  The classes write disjoint cells and read
-  // only the step's inputs, so their order does not matter.
+  // class (by the tissue's largest ring), the largest rings first on the
+  // auxiliary stream and the smallest on `s`, joined back into `s`.  The
+  // classes write disjoint cells and read only the step's inputs, so their
+  // order does not matter.
   cudaError_t launch_step(const Step2DArgs &a0, cudaStream_t s) {
     if (serving || nclass <= 1) return launch_step2d(a0, maxnv, warps, variant(), s);
     cudaError_t e = cudaEventRecord(ev_fork, s);
@@ -368,17 +370,31 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
     }
     if (off > (1L << 31) - 1) return fail(DPM_ECAPACITY, "too many vertices");
     b->nverts = off;
-    // vertex-slot classes and the cells of each, in cell order
+    // vertex-slot classes and the cells of each, in cell order.  A cell's
+    // class is that of the largest ring of its TISSUE: the step holds the
+    // neighbours' rings (cells of the same tissue) in the same slots as its
+    // own, so every cell of a tissue runs the code of the tissue's largest
+    // ring.
     auto slot_class = [](unsigned v) { return v <= 32 ? 0 : v <= 64 ? 1 : v <= 128 ? 2 : 3; };
+    std::vector<unsigned char> cls(total_cells);
+    {
+      long c0 = 0;
+      for (int t = 0; t < ntissues; ++t) {
+        unsigned m = 0;
+        for (long c = c0; c < c0 + ncells[t]; ++c) m = std::max(m, nv[c]);
+        for (long c = c0; c < c0 + ncells[t]; ++c) cls[c] = (unsigned char)slot_class(m);
+        c0 += ncells[t];
+      }
+    }
     int cnt[4] = {0, 0, 0, 0};
-    for (long c = 0; c < total_cells; ++c) ++cnt[slot_class(nv[c])];
+    for (long c = 0; c < total_cells; ++c) ++cnt[cls[c]];
     b->nclass = (cnt[0] > 0) + (cnt[1] > 0) + (cnt[2] > 0) + (cnt[3] > 0);
     std::vector<int> order;
     if (b->nclass > 1) {
       for (int k = 0; k < 4; ++k) b->class_begin[k + 1] = b->class_begin[k] + cnt[k];
       order.resize(total_cells);
       int fill[4] = {b->class_begin[0], b->class_begin[1], b->class_begin[2], b->class_begin[3]};
-      for (long c = 0; c < total_cells; ++c) order[fill[slot_class(nv[c])]++] = (int)c;
+      for (long c = 0; c < total_cells; ++c) order[fill[cls[c]]++] = (int)c;
     }
     b->h_cells.resize(total_cells);
     b->h_Ka.assign(total_cells, 0.0f);

@@ -160,6 +160,37 @@ def test_batched_equals_alone(ctx):
         off += nvt
 
 
+def test_mixed_slot_classes(ctx):
+    """Tissues of different ring sizes in one batch run one kernel per
+    vertex-slot class; a tissue with rings of 16 and 48 vertices belongs to
+    the class of its largest ring (its cells hold neighbours of 48).  Every
+    tissue equals itself alone, bit for bit, and the oracle (one step: flags
+    identical, forces within tolerance)."""
+    rng = np.random.default_rng(5)
+    specs = [(24, rng.choice([16, 48], size=24), 0.5), (30, 16, 0.0), (20, 24, 0.3),
+             (18, rng.choice([16, 24, 32], size=18), 0.0), (9, 100, 0.0)]
+    states = [make_tissue2d(n, nv, r0=rng.uniform(0.9, 1.3, n), calA=rng.uniform(1.0, 1.2, n),
+                            Kb=0.02, phi=0.82, Kat=kat, seed=60 + k)
+              for k, (n, nv, kat) in enumerate(specs)]
+    b = gpu_batch2d(ctx, states)
+    b.step(1, DT)
+    xy, F = b.download()
+    flags = b.contained()
+    b.step(29, DT)
+    xy30, _ = b.download()
+    off = 0
+    for s in states:
+        nvt = int(s.nv.sum())
+        rx, rF, rflags = oracle_run(s, 1)
+        assert np.array_equal(flags[off:off + nvt], rflags)
+        assert rel_norm_err(F[off:off + nvt], rF) <= F_TOL
+        a = gpu_batch2d(ctx, [s])
+        a.step(30, DT)
+        ax, _ = a.download()
+        assert np.array_equal(ax, xy30[off:off + nvt])
+        off += nvt
+
+
 def test_deterministic(ctx):
     s = make_tissue2d(64, 32, phi=0.85, seed=13, Kb=0.01)
     out = []
