@@ -334,15 +334,23 @@ def profile_rows(summary):
     return out
 
 
-def launches_per_call(batch, sim_steps, period):
+def slot_classes(tissues):
+    """Vertex-slot classes of a batch (one step launch each): the class of a
+    tissue is that of its largest ring (<= 32, 64, 128, 256 vertices)."""
+    return len({min(3, max(0, math.ceil(math.log2(int(t["nv"].max()) / 32))))
+                for t in tissues})
+
+
+def launches_per_call(batch, tissues, sim_steps, period):
     """Kernel launches of one dpm2d_step(sim_steps): per rebuild period one
     bin-preparation launch, 3 launches per radix pass, one neighbour-list
-    launch; one fused step launch per simulation step."""
+    launch; per simulation step one fused step launch per vertex-slot
+    class."""
     lb, _, _, _ = batch.bins()
     tbits = int(math.ceil(math.log2(batch.ntissues))) if batch.ntissues > 1 else 0
     passes = (lb + tbits + 7) // 8
     blocks = math.ceil(sim_steps / period)
-    return blocks * (1 + 3 * passes + 1) + sim_steps
+    return blocks * (1 + 3 * passes + 1) + sim_steps * slot_classes(tissues)
 
 
 def reduce_over_ranks(secs, units, world, device):
@@ -468,7 +476,8 @@ def run_ours(args, rank, world, local_rank):
         "config": sweep_config(b.ntissues, N, V),
         "graph": "one CUDA graph replay per cell-list rebuild period",
         "tuning": tuned,
-        "gpu_launches": launches_per_call(b, SIM_STEPS, tuned["rebuild_period"]) * args.steps,
+        "gpu_launches": launches_per_call(b, tissues, SIM_STEPS,
+                                          tuned["rebuild_period"]) * args.steps,
         "roofline": roofline, "e2e": e2e, "same_sample": sample,
         "plain": c1,
         "batched_over_plain": round(value / world / c1["value"], 2),
