@@ -207,9 +207,10 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache,
  *     DPM_NOALLOC_MAX_VERTICES, 3..256 vertices per cell; larger inputs are
  *     rejected with DPM_ECAPACITY;
  *   - every call shares that array, and its contents are not valid between
- *     calls.  Calls are serialized by a process-wide lock (calls on
- *     different devices too), and each returns only after its work is done,
- *     so calls from several host threads never overlap inside the library;
+ *     calls.  Calls that overlapped on the GPU would race on it; the library
+ *     serializes calls with a process-wide lock (calls on different devices
+ *     too), and each returns only after its work is done, so calls from
+ *     several host threads never overlap inside the library;
  *   - the first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) once and keeps it for the life of the process:
  *     do not reset the device (cudaDeviceReset) between calls, and call from
