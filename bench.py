@@ -979,11 +979,23 @@ def cpu_baselines_plain(geo, budget_s=10.0):
         P.run3d(s, 1, DT3, nthreads=thr)
         res[name] = round(s.xyz.shape[0] / (time.perf_counter() - t0), 1)
         res[name + "_cells"] = ncell
+    # the variant the reference itself can run: subdivision 2 (162 vertices)
+    for name, ncell, thr in (("sub2_all_cores", 128, cores), ("sub2_single_thread", 16, 1)):
+        t = build_monolayer(clDPM, np.random.default_rng(4), ncell, 2)
+        s = Tissue3DState(nv=t["nv"], faces=t["faces"], xyz=t["xyz"].copy(), Kv=t["Kv"],
+                          Ka=t["Ka"], Ks=t["Ks"], v0=t["v0"], a0=t["a0"], l0=t["l0"],
+                          L=float(t["L"]), Kre=1.0, pbc=1, Kb=t["Kb"], adh=t["adh"])
+        t0 = time.perf_counter()
+        P.run3d(s, 1, DT3, nthreads=thr)
+        res[name] = round(s.xyz.shape[0] / (time.perf_counter() - t0), 1)
+        res[name + "_cells"] = ncell
     out["c2"] = dict(res, steps=1,
                      sample="monolayers of 32 (all cores) and 8 (one thread) cells x 642 "
-                            "vertices (subdivision 3), one step; the oracle's winding sum runs "
-                            "over all cell pairs, so the 256-cell rate is ~8x below the 32-cell "
-                            "one")
+                            "vertices (subdivision 3), and of 128 and 16 cells x 162 vertices "
+                            "(subdivision 2, the reference's own mesh), one step each; the "
+                            "oracle's winding sum runs over all cell pairs, so a 256-cell "
+                            "monolayer runs ~8x (subdivision 3) or ~2x (subdivision 2) slower "
+                            "per vertex than these samples")
     return out
 
 

@@ -113,9 +113,12 @@ int dpm2d_sizes(dpm2d_batch *b, int *ncells, long *nvertices);
  * in steps (even) and skin distance relative to the mean cell radius. */
 int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel,
                      int warps_per_block);
-/* Step-kernel variant 0..3 (bit 0: registers capped for 32 resident warps
- * per SM; bit 1: dynamic schedule).  Every variant gives identical results;
- * dpm2d_autotune picks the fastest. */
+/* Step-kernel variant 0..3 (bit 0: registers capped for 48 resident warps
+ * per SM; bit 1: dynamic schedule), plus 8 to switch off the resident run:
+ * batches whose tissues are all small (at most 64 cells and 2,048 vertices,
+ * rings of at most 64) otherwise step with one block per tissue holding the
+ * tissue in shared memory for the whole call.  Every variant gives identical
+ * results; dpm2d_autotune picks the fastest graph-path variant. */
 int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant);
 
 /* Diagnostics: per-vertex containment flags of the last step (uint8 per

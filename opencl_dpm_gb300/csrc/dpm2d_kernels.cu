@@ -466,6 +466,17 @@ cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStrea
   return cudaGetLastError();
 }
 
+size_t resident2d_smem_bytes(int ncmax, int nvmax) {
+  return 128 + sizeof(Cell2D) * (size_t)ncmax + 2 * sizeof(Geom2D) * (size_t)ncmax +
+         2 * sizeof(float2) * (size_t)nvmax;
+}
+
+cudaError_t launch_resident2d(const Resident2DArgs &r, int ntissues, int maxnv, int variant,
+                              cudaStream_t s) {
+  if (maxnv <= 32) return launch_resident2d_s1(r, ntissues, variant, s);
+  return launch_resident2d_s2(r, ntissues, variant, s);
+}
+
 cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int occ, cudaStream_t s) {
   if (maxnv <= 32) return launch_step2d_s1(a, warps, occ, s);
   if (maxnv <= 64) return launch_step2d_s2(a, warps, occ, s);

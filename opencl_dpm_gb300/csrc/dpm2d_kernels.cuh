@@ -72,6 +72,33 @@ cudaError_t launch_neighbors2d(const Rebuild2DArgs &a, int local_bits, cudaStrea
 // is smaller and faster).
 cudaError_t launch_step2d(const Step2DArgs &a, int maxnv, int warps, int variant,
                           cudaStream_t s);
+// Resident run of small tissues (k2d_run_resident): one block per tissue
+// keeps the tissue in shared memory for `nsteps` steps.  `a` carries the
+// cells, tissues, outputs (forces and flags of the last step), geom0, nn, err,
+// dt and all_forces of an ordinary step; pos and geom are the batch's current
+// positions and their geometry, read at the start and written at the end.
+struct Resident2DArgs {
+  Step2DArgs a;
+  float2 *pos;
+  Geom2D *geom;
+  int nsteps;
+  int ncmax;  // largest tissue: cells and vertices (sizes the shared memory)
+  int nvmax;
+};
+constexpr int kResidentWarps = 16;
+// Tissues that take the resident run: at most this many cells and vertices.
+constexpr int kResidentMaxCells = 64;
+constexpr int kResidentMaxVerts = 2048;
+// Dynamic shared memory of one block of the resident run.
+size_t resident2d_smem_bytes(int ncmax, int nvmax);
+// Launches the resident run over tissues [0, ntissues) (variant bit 2: the
+// attraction compiled in); maxnv <= 64.
+cudaError_t launch_resident2d(const Resident2DArgs &r, int ntissues, int maxnv, int variant,
+                              cudaStream_t s);
+cudaError_t launch_resident2d_s1(const Resident2DArgs &r, int ntissues, int variant,
+                                 cudaStream_t s);
+cudaError_t launch_resident2d_s2(const Resident2DArgs &r, int ntissues, int variant,
+                                 cudaStream_t s);
 // The same for 32*S vertex slots per warp (dpm2d_step_s<S>.cu).
 cudaError_t launch_step2d_s1(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
 cudaError_t launch_step2d_s2(const Step2DArgs &a, int warps, int variant, cudaStream_t s);

@@ -433,6 +433,103 @@ __global__ void __launch_bounds__(W * 32, (StepOcc<S, W, OCC>::kBlocks))
   }
 }
 
+// Resident run of small tissues: one block per tissue copies the tissue's
+// constants, positions and geometry into shared memory (cell ids, vertex
+// offsets and the tissue id made local), runs nsteps steps there -- its warps
+// take the tissue's cells in turn, the block synchronizes between steps --
+// and writes the positions and geometry back.  The stale flag is held set,
+// so every cell screens the whole tissue in ascending order: the pairs and
+// their order are those of the neighbour lists, whose pruning is exact, and
+// the results are the graph path's bit for bit.  For tissues too small to
+// fill the GPU, where a step of the graph path waits on launch and global
+// memory latency.
+template <int S, bool ATT>
+__global__ void __launch_bounds__(kResidentWarps * 32)
+    k2d_run_resident(Resident2DArgs r) {
+  constexpr int M = 32 * S, W = kResidentWarps;
+  __shared__ float sh_x[W][M], sh_y[W][M], sh_nx[W][M], sh_ny[W][M];
+  __shared__ unsigned char sh_f[W][M];
+  __shared__ int sh_stale;
+  extern __shared__ __align__(16) unsigned char res_smem[];
+  Tissue2D *ts = reinterpret_cast<Tissue2D *>(res_smem);
+  Cell2D *cs = reinterpret_cast<Cell2D *>(res_smem + 128);
+  Geom2D *gs0 = reinterpret_cast<Geom2D *>(cs + r.ncmax);
+  Geom2D *gs1 = gs0 + r.ncmax;
+  float2 *ps0 = reinterpret_cast<float2 *>(gs1 + r.ncmax);
+  float2 *ps1 = ps0 + r.nvmax;
+  const int t = blockIdx.x;
+  const Tissue2D T = r.a.tissues[t];
+  const int c0 = T.cell_begin, nc = T.cell_end - T.cell_begin;
+  const uint32_t v0 = r.a.cells[c0].voff;
+  const int nvt = (int)(r.a.cells[c0 + nc - 1].voff + r.a.cells[c0 + nc - 1].nv - v0);
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    Cell2D cp = r.a.cells[c0 + i];
+    cp.voff -= v0;
+    cp.tissue = 0;
+    cs[i] = cp;
+    gs0[i] = r.geom[c0 + i];
+  }
+  for (int i = threadIdx.x; i < nvt; i += blockDim.x) ps0[i] = r.pos[v0 + i];
+  if (threadIdx.x == 0) {
+    Tissue2D tl = T;
+    tl.cell_begin = 0;
+    tl.cell_end = nc;
+    *ts = tl;
+    sh_stale = 1;  // screen the whole tissue at every step
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Step2DArgs a = r.a;
+  a.cells = cs;
+  a.tissues = ts;
+  a.geom0 = r.a.geom0 + c0;
+  a.nn = r.a.nn + c0;
+  a.stale = &sh_stale;
+  a.step_index = 0;
+  a.order = nullptr;
+  float2 *pin = ps0, *pout = ps1;
+  Geom2D *gin = gs0, *gout = gs1;
+  for (int step = 0; step < r.nsteps; ++step) {
+    const bool last = step == r.nsteps - 1;
+    a.pos_in = pin;
+    a.pos_out = pout;
+    a.geom_in = gin;
+    a.geom_out = gout;
+    a.force_out = last && r.a.force_out ? r.a.force_out + v0 : nullptr;
+    a.flags_out = last && r.a.flags_out ? r.a.flags_out + v0 : nullptr;
+    for (int c = w; c < nc; c += W)
+      step_cell<S, ATT>(a, c, lane, sh_x[w], sh_y[w], sh_nx[w], sh_ny[w], sh_f[w]);
+    __syncthreads();
+    float2 *tp = pin;
+    pin = pout;
+    pout = tp;
+    Geom2D *tg = gin;
+    gin = gout;
+    gout = tg;
+  }
+  for (int i = threadIdx.x; i < nvt; i += blockDim.x) r.pos[v0 + i] = pin[i];
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) r.geom[c0 + i] = gin[i];
+}
+
+template <int S, bool ATT>
+cudaError_t launch_resident_sa(const Resident2DArgs &r, int ntissues, cudaStream_t s) {
+  const size_t bytes = resident2d_smem_bytes(r.ncmax, r.nvmax);
+  // the dynamic shared-memory limit of the kernel, raised once to what any
+  // resident run may use
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      k2d_run_resident<S, ATT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      (int)resident2d_smem_bytes(kResidentMaxCells, kResidentMaxVerts));
+  if (attr != cudaSuccess) return attr;
+  k2d_run_resident<S, ATT><<<ntissues, kResidentWarps * 32, bytes, s>>>(r);
+  return cudaGetLastError();
+}
+
+template <int S>
+cudaError_t launch_resident_s(const Resident2DArgs &r, int ntissues, int variant, cudaStream_t s) {
+  return (variant & kStepVariantAttraction) ? launch_resident_sa<S, true>(r, ntissues, s)
+                                            : launch_resident_sa<S, false>(r, ntissues, s);
+}
+
 template <int S, int W, int OCC, bool ATT>
 cudaError_t launch_step_sw(const Step2DArgs &a, bool dyn, cudaStream_t s) {
   if (dyn && a.sched) {

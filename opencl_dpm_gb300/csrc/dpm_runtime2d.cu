@@ -102,6 +102,13 @@ struct dpm2d_batch {
   // tissue runs the code compiled for its ring sizes.
   int nclass = 1;
   int class_begin[5] = {0, 0, 0, 0, 0};
+
+  // Resident run (k2d_run_resident): batches whose tissues are all small
+  // (at most kResidentMaxCells cells and kResidentMaxVerts vertices, rings of
+  // at most 64) step with one block per tissue holding it in shared memory
+  // for a whole call, unless switched off (variant bit 3).
+  bool resident_fits = false, no_resident = false;
+  int res_ncmax = 0, res_nvmax = 0;
   int *d_order = nullptr;
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -252,6 +259,27 @@ struct dpm2d_batch {
     return cudaSuccess;
   }
 
+  bool resident() const { return resident_fits && !no_resident && !serving; }
+
+  // A call of nsteps on the resident run: launches of up to 4096 steps each;
+  // the positions and geometry stay in buffer `cur`.
+  int run_resident(int nsteps, float dt) {
+    constexpr int kChunk = 4096;
+    for (int done = 0; done < nsteps;) {
+      const int len = std::min(kChunk, nsteps - done);
+      Resident2DArgs r{};
+      r.a = step_args(cur, dt, done + len == nsteps, 0);
+      r.pos = d_pos[cur];
+      r.geom = d_geom[cur];
+      r.nsteps = len;
+      r.ncmax = res_ncmax;
+      r.nvmax = res_nvmax;
+      DPM_CUDA_TRY(launch_resident2d(r, ntissues, maxnv, variant(), stream));
+      done += len;
+    }
+    return DPM_OK;
+  }
+
   int run_block(int len, float dt, bool last) {
     cudaStream_t s = stream;
     uint32_t dtbits;
@@ -385,6 +413,19 @@ int dpm2d_create(dpm_ctx *ctx, int ntissues, const int *ncells, const unsigned *
         for (long c = c0; c < c0 + ncells[t]; ++c) cls[c] = (unsigned char)slot_class(m);
         c0 += ncells[t];
       }
+    }
+    {
+      long c0 = 0;
+      bool fits = b->maxnv <= 64;
+      for (int t = 0; t < ntissues; ++t) {
+        long v = 0;
+        for (long c = c0; c < c0 + ncells[t]; ++c) v += nv[c];
+        fits = fits && ncells[t] <= kResidentMaxCells && v <= kResidentMaxVerts;
+        b->res_ncmax = std::max(b->res_ncmax, ncells[t]);
+        b->res_nvmax = std::max(b->res_nvmax, (int)v);
+        c0 += ncells[t];
+      }
+      b->resident_fits = fits;
     }
     int cnt[4] = {0, 0, 0, 0};
     for (long c = 0; c < total_cells; ++c) ++cnt[cls[c]];
@@ -604,8 +645,10 @@ int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel, int war
 
 int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant) {
   if (int r = check_batch(b)) return r;
-  if (variant < 0 || variant > 3) return fail(DPM_EINVAL, "step-kernel variant must be 0..3");
-  b->occ = variant;
+  if (variant < 0 || (variant & ~11) != 0)
+    return fail(DPM_EINVAL, "step-kernel variant must be 0..3, plus 8 to switch off the resident run");
+  b->occ = variant & 3;
+  b->no_resident = (variant & 8) != 0;
   b->clear_graphs();
   return DPM_OK;
 }
@@ -645,6 +688,7 @@ int dpm2d_step(dpm2d_batch *b, int nsteps, float dt) {
   if (!std::isfinite(dt)) return fail(DPM_EINVAL, "dt must be finite");
   if (nsteps == 0) return DPM_OK;
   cudaSetDevice(b->ctx->device);
+  if (b->resident()) return b->run_resident(nsteps, dt);
   const int R = b->rebuild_period;
   const int full = nsteps / R, rem = nsteps % R;
   for (int i = 0; i < full; ++i)

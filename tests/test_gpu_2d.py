@@ -243,7 +243,7 @@ def test_kernel_variants_identical(ctx):
                             phi=float(rng.uniform(0.6, 0.9)), Kb=0.01, seed=200 + t)
               for t in range(5)]
     out = {}
-    for variant in range(4):
+    for variant in (0, 1, 2, 3, 8, 11):
         for warps in (4, 8, 16):
             b = gpu_batch2d(ctx, states, dict(warps=warps))
             b.set_kernel_variant(variant)
@@ -253,6 +253,36 @@ def test_kernel_variants_identical(ctx):
     ref = out[(1, 8)]
     for k, (xy, F) in out.items():
         assert np.array_equal(xy, ref[0]) and np.array_equal(F, ref[1]), k
+
+
+def test_resident_run_same_bits(ctx):
+    """Batches of small tissues step with one block per tissue held in
+    shared memory for the whole call; that run equals the graph path (variant
+    bit 3 switches it off) bit for bit -- positions, last-step forces and
+    containment flags -- with ragged rings, attraction, and a call longer
+    than one resident launch (4,096 steps)."""
+    rng = np.random.default_rng(41)
+    states = [make_tissue2d(16, 32, phi=0.6, seed=300),
+              make_tissue2d(40, rng.choice([16, 24, 32, 48], size=40), r0=rng.uniform(0.9, 1.3, 40),
+                            calA=rng.uniform(1.0, 1.2, 40), Kb=0.02, phi=0.85, Kat=0.4, seed=301),
+              make_tissue2d(9, 20, calA=1.1, phi=0.8, seed=302)]
+    for nsteps in (1, 37, 4100):
+        res = []
+        for variant in (3, 11):
+            b = gpu_batch2d(ctx, states)
+            b.set_kernel_variant(variant)
+            b.step(nsteps, DT)
+            xy, F = b.download()
+            res.append((xy, F, b.contained()))
+        assert all(np.array_equal(u, v) for u, v in zip(res[0], res[1])), nsteps
+    # and the oracle, one step from a perturbed state
+    s = perturb(states[1], 0.05, 7)
+    b = gpu_batch2d(ctx, [s])
+    b.step(1, DT)
+    _, F = b.download()
+    _, rF, rflags = oracle_run(s, 1)
+    assert np.array_equal(b.contained(), rflags)
+    assert rel_norm_err(F, rF) <= F_TOL
 
 
 def test_attraction_variant_same_bits(ctx):
