@@ -1047,7 +1047,8 @@ def run_profile(kind):
     benchmark, then the launches to capture run inside the NVTX range
     "profile" (ncu --nvtx --nvtx-include "profile/"): for "2d" one fused step
     of the batched sweep (one launch per vertex-slot class) after a fresh
-    neighbour-list rebuild; for "3d" one step of the 256-cell monolayer."""
+    neighbour-list rebuild; for "3d" one step of the 256-cell monolayer, for
+    "3d48" one step of the 48 monolayers of the batched 3D leg."""
     import torch
     from opencl_dpm_gb300.abi import Context
     ctx = Context(0)
@@ -1064,8 +1065,12 @@ def run_profile(kind):
         torch.cuda.nvtx.range_pop()
     else:
         from opencl_dpm_gb300 import clDPM
-        t = build_monolayer(clDPM, np.random.default_rng(3), 256, 3)
-        b = make_batch3d(ctx, [t])
+        if kind == "3d48":
+            rng = np.random.default_rng(5)
+            ts = [build_monolayer(clDPM, rng, int(rng.integers(8, 65)), 3) for _ in range(48)]
+        else:
+            ts = [build_monolayer(clDPM, np.random.default_rng(3), 256, 3)]
+        b = make_batch3d(ctx, ts)
         for _ in range(3):
             b.step(16, DT3)
         ctx.synchronize()
@@ -1085,7 +1090,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests in the served mixed stream (0 skips it)")
-    ap.add_argument("--profile", choices=["2d", "3d"], default=None,
+    ap.add_argument("--profile", choices=["2d", "3d", "3d48"], default=None,
                     help="run only a profiling target (see run_profile)")
     args = ap.parse_args()
     if args.profile:
