@@ -135,7 +135,13 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
                                                          fabsf(gl.cx) + fabsf(gl.cy));
         // own y range must meet (miny_j, maxy_j] unless y offsets can shift
         const bool yover = gi.maxy > gl.miny && gi.miny <= gl.maxy;
-        const bool near = yover && dcx * dcx + dcy * dcy <= (rr + mm) * (rr + mm);
+        // and its x range must meet the widened box of j: a vertex's box
+        // test (vertex_candidate) widens by at most this margin
+        const float bmx = kRelMargin * (gl.maxx - gl.minx) +
+                          kAbsMargin * (fabsf(gl.minx) + fabsf(gl.maxx) +
+                                        fmaxf(fabsf(gi.minx), fabsf(gi.maxx)));
+        const bool xover = gi.maxx >= gl.minx - bmx && gi.minx <= gl.maxx + bmx;
+        const bool near = yover && xover && dcx * dcx + dcy * dcy <= (rr + mm) * (rr + mm);
         const bool farx = pbc && (__fsub_rn(gi.maxx, gl.minx) > L || __fsub_rn(gl.maxx, gi.minx) > L);
         const bool fary = pbc && (__fsub_rn(gi.maxy, gl.miny) > L || __fsub_rn(gl.maxy, gi.miny) > L);
         const bool far = fary || (farx && yover);

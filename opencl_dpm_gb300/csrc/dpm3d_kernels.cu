@@ -174,15 +174,12 @@ struct Smem3D {
   unsigned *near;
   uint16_t *faces, *cand, *pvert, *nlist, *defer;
   float *terms; // [2][nf] face terms of a deferred candidate
-  // the staged neighbour's vertices once more, in patch order (entry i is
-  // vertex pvert[i]), so a patch walk reads coordinates without the id first
-  float *rx, *ry, *rz;
   float *ex, *ey, *ez, *eL; // unit vector (lower id -> higher id) and length of each edge
   unsigned char *wnc;
 };
 
 __host__ __device__ __forceinline__ int q_region(int nv, int nf, int ne) {
-  const int a = 6 * nv + 2 * nf, b = 4 * ne;
+  const int a = 3 * nv + 2 * nf, b = 4 * ne;
   return a > b ? a : b;
 }
 
@@ -203,9 +200,6 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool
   s.qy = f + nv;
   s.qz = f + 2 * nv;
   s.terms = f + 3 * nv;
-  s.rx = f + 3 * nv + 2 * nf;
-  s.ry = s.rx + nv;
-  s.rz = s.ry + nv;
   s.ex = f;
   s.ey = f + ne;
   s.ez = f + 2 * ne;
@@ -333,7 +327,7 @@ __device__ __forceinline__ bool face_plane_separates(const Smem3D &s, const Mesh
     const int p = __ffs(todo) - 1;
     todo &= todo - 1u;
     const int o = s.poff[p], cnt = s.poff[p + 1] - o;
-    if (lane < cnt) bad |= !(dot(mk(s.rx[o + lane], s.ry[o + lane], s.rz[o + lane]) - pt, n) < -M);
+    if (lane < cnt) bad |= !(dot(nbv(s, s.pvert[o + lane]) - pt, n) < -M);
   }
   return !__any_sync(kFull, bad);
 }
@@ -397,7 +391,7 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
       int k = 0;
       if (lane < n) {
         k = s.pvert[o + lane];
-        const f3 q = mk(s.rx[o + lane], s.ry[o + lane], s.rz[o + lane]);
+        const f3 q = nbv(s, k);
         h = fmaxf(h, dot(q - cj, u));
         const f3 d = q - pt;
         nr = dot(d, d) <= dn2;
@@ -522,9 +516,8 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
 
 // Two blocks per SM by registers (64 a thread, no spills).
 // Stages cell j's vertices, shifted to the periodic image nearest this cell,
-// into s.q* (vertex order) and s.r* (patch order), and the bounding spheres
-// of its patches, from the same shifted coordinates, into s.pb (the whole
-// block; no barrier).
+// into s.q*, and the bounding spheres of its patches, from the same shifted
+// coordinates, into s.pb (the whole block; no barrier).
 __device__ __forceinline__ void stage_neighbour(const Smem3D &s, const Step3DArgs &a, int j,
                                                 f3 shift, int NV, int NP, int tid, int w,
                                                 int lane) {
@@ -533,10 +526,6 @@ __device__ __forceinline__ void stage_neighbour(const Smem3D &s, const Step3DArg
     s.qx[k] = a.xin[bj + k] + shift.x;
     s.qy[k] = a.yin[bj + k] + shift.y;
     s.qz[k] = a.zin[bj + k] + shift.z;
-    const int kp = s.pvert[k];
-    s.rx[k] = a.xin[bj + kp] + shift.x;
-    s.ry[k] = a.yin[bj + kp] + shift.y;
-    s.rz[k] = a.zin[bj + kp] + shift.z;
   }
   for (int p = w; p < NP; p += kWarps) {
     const int o = s.poff[p], n = s.poff[p + 1] - o;
