@@ -117,8 +117,11 @@ int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel,
  * per SM; bit 1: dynamic schedule), plus 8 to switch off the resident run:
  * batches whose tissues are all small (at most 64 cells and 2,048 vertices,
  * rings of at most 64) otherwise step with one block per tissue holding the
- * tissue in shared memory for the whole call.  Every variant gives identical
- * results; dpm2d_autotune picks the fastest graph-path variant. */
+ * tissue in shared memory for the whole call; plus 32 for four warps per
+ * cell that split the cell's neighbours (batches without attraction whose
+ * rings have at most 64 vertices; for batches too small to fill the GPU).
+ * Every variant gives identical results; dpm2d_autotune picks the fastest
+ * graph-path variant. */
 int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant);
 
 /* Diagnostics: per-vertex containment flags of the last step (uint8 per

@@ -99,6 +99,11 @@ cudaError_t launch_resident2d_s1(const Resident2DArgs &r, int ntissues, int vari
                                  cudaStream_t s);
 cudaError_t launch_resident2d_s2(const Resident2DArgs &r, int ntissues, int variant,
                                  cudaStream_t s);
+// One step with a team of 4 warps per cell (no attraction; maxnv <= 64;
+// variant bit 0: register cap).
+cudaError_t launch_team2d_s1(const Step2DArgs &a, int variant, cudaStream_t s);
+cudaError_t launch_team2d_s2(const Step2DArgs &a, int variant, cudaStream_t s);
+constexpr int kStepVariantTeam = 32;
 // The same for 32*S vertex slots per warp (dpm2d_step_s<S>.cu).
 cudaError_t launch_step2d_s1(const Step2DArgs &a, int warps, int variant, cudaStream_t s);
 cudaError_t launch_step2d_s2(const Step2DArgs &a, int warps, int variant, cudaStream_t s);

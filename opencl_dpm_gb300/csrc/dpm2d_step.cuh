@@ -28,10 +28,19 @@ template <int S, int W, int OCC> struct StepOcc {
 
 // One step of cell c by one warp; (sx, sy), (nxs, nys) and sf are the warp's
 // shared-memory ring, neighbour ring and containment flags (32*S entries).
-template <int S, bool ATT>
+//
+// TEAM > 1: the TEAM warps of a block step the cell together (no
+// attraction).  Warp `team` 0 forms the shape forces and, after the block's
+// barrier, the repulsion toward the own centre, the Euler update and the
+// next step's geometry; every warp screens the list and takes every TEAM-th
+// passing neighbour, OR-ing containment flags into the block's sf.  A flag
+// is the OR over neighbours, so the result does not depend on which warp
+// took which neighbour: the same bits as one warp.
+template <int S, bool ATT, int TEAM = 1>
 __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, const int lane,
                                           float *sx, float *sy, float *nxs, float *nys,
-                                          unsigned char *sf) {
+                                          unsigned char *sf, const int team = 0) {
+  static_assert(TEAM == 1 || !ATT, "the attraction adds forces in list order: one warp");
   const Cell2D cp = a.cells[c];
   const int n = (int)cp.nv;
   if (n == 0) return;  // an empty slot
@@ -39,6 +48,7 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
   const Tissue2D T = a.tissues[tid];
   if (a.step_index >= T.run_now) {
     // the tissue's step budget is spent: carry its state over unchanged
+    if (team != 0) return;
     for (int k = lane; k < n; k += 32) a.pos_out[cp.voff + k] = a.pos_in[cp.voff + k];
     if (lane == 0) a.geom_out[c] = a.geom_in[c];
     return;
@@ -58,12 +68,15 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
       const float2 v = a.pos_in[cp.voff + k];
       vx[s] = v.x;
       vy[s] = v.y;
-      sx[k] = v.x;
-      sy[k] = v.y;
-      sf[k] = 0;
+      if (team == 0) {
+        sx[k] = v.x;
+        sy[k] = v.y;
+        sf[k] = 0;
+      }
     }
   }
-  __syncwarp();
+  if constexpr (TEAM > 1) __syncthreads();
+  else __syncwarp();
   const Geom2D gi = a.geom_in[c];
 
   // -- shape forces: area (AreaForceUpdates, with the reference's sign of
@@ -74,7 +87,7 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
 #pragma unroll
   for (int s = 0; s < S; ++s) {
     const int k = lane + 32 * s;
-    if (k < n) {
+    if (k < n && team == 0) {
       const int im1 = k == 0 ? n - 1 : k - 1;
       const int ip1 = k == n - 1 ? 0 : k + 1;
       const int im2 = im1 == 0 ? n - 1 : im1 - 1;
@@ -109,6 +122,7 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
   const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
   const int *list = a.nbr + (size_t)c * kMaxNB2D;
   const bool att = ATT && T.Kat != 0.0f;
+  int ordinal = 0;  // passing neighbours seen (team mode)
   // Lanes screen up to 32 list entries at once (one geometry load each, in
   // parallel); the cells that pass are then processed one by one, in list
   // order, with their geometry broadcast by shuffles.
@@ -162,6 +176,12 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     while (pm) {
     const int src = __ffs(pm) - 1;
     pm &= pm - 1u;
+    if constexpr (TEAM > 1) {
+      // every TEAM-th passing neighbour, in list order, is this warp's
+      const bool mine = ordinal % TEAM == team;
+      ++ordinal;
+      if (!mine) continue;
+    }
     const unsigned fl = __shfl_sync(kFull, pflags, src);
     const unsigned jx = __shfl_sync(kFull, jvoff, src), jy = __shfl_sync(kFull, jnv, src);
     const bool near = fl & 1u, far = fl & 2u, attp = fl & 4u;
@@ -343,6 +363,11 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
     }
     __syncwarp();
     }
+  }
+
+  if constexpr (TEAM > 1) {
+    __syncthreads();  // every warp's flags are in sf
+    if (team != 0) return;
   }
 
   // -- repulsion force toward the own centre (Cell2D_kernel.cl:205-219)
@@ -534,6 +559,58 @@ template <int S>
 cudaError_t launch_resident_s(const Resident2DArgs &r, int ntissues, int variant, cudaStream_t s) {
   return (variant & kStepVariantAttraction) ? launch_resident_sa<S, true>(r, ntissues, s)
                                             : launch_resident_sa<S, false>(r, ntissues, s);
+}
+
+// Team schedule (no attraction): TEAM warps per block step one cell
+// together (see step_cell), the blocks taking cells from the counter.  For
+// batches too small to fill the GPU with one warp per cell, where a cell's
+// step is a long chain of dependent loads: its neighbours are split over
+// more warps.  The last block to finish resets the counters.
+template <int S, int TEAM, int OCC>
+__global__ void __launch_bounds__(TEAM * 32, (StepOcc<S, TEAM, OCC>::kBlocks))
+    k2d_step_team(Step2DArgs a) {
+  constexpr int M = 32 * S;
+  __shared__ float sh_x[M], sh_y[M];
+  __shared__ unsigned char sh_f[M];
+  __shared__ int sh_i;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    if (threadIdx.x == 0) sh_i = atomicAdd(a.sched, 1);
+    __syncthreads();
+    const int i = sh_i;
+    __syncthreads();  // read by every thread before the next fetch
+    if (i >= a.ncells) break;
+    const int c = a.order ? a.order[i] : i;
+    step_cell<S, false, TEAM>(a, c, lane, sh_x, sh_y, nullptr, nullptr, sh_f, w);
+  }
+  if (threadIdx.x == 0 && atomicAdd(a.sched + 1, 1) == (int)gridDim.x - 1) {
+    atomicExch(a.sched, 0);
+    atomicExch(a.sched + 1, 0);
+  }
+}
+
+template <int S, int TEAM, int OCC>
+cudaError_t launch_team_so(const Step2DArgs &a, cudaStream_t s) {
+  static const int per_sm_sms = [] {
+    int per = 0, dev = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k2d_step_team<S, TEAM, OCC>,
+                                                      TEAM * 32, 0) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+    return (per < 1 ? 1 : per) * (sms < 1 ? 1 : sms);
+  }();
+  if (per_sm_sms <= 0) return cudaErrorUnknown;
+  const int grid = a.ncells < per_sm_sms ? a.ncells : per_sm_sms;
+  if (grid <= 0) return cudaSuccess;
+  k2d_step_team<S, TEAM, OCC><<<grid, TEAM * 32, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// variant bit 0: register cap for occupancy (the team is always 4 warps)
+template <int S>
+cudaError_t launch_team_s(const Step2DArgs &a, int variant, cudaStream_t s) {
+  return (variant & 1) ? launch_team_so<S, 4, 1>(a, s) : launch_team_so<S, 4, 0>(a, s);
 }
 
 template <int S, int W, int OCC, bool ATT>

@@ -123,6 +123,7 @@ struct dpm2d_batch {
   int warps = 8;
   int occ = 1;
   bool att = false;     // some tissue has Kat != 0: launch the step with attraction
+  bool team = false;    // variant bit 5: four warps per cell (no attraction, rings <= 64)
   bool serving = false; // slot pool of a server: per-tissue step budgets
   long rebuilds = 0;
 
@@ -221,13 +222,23 @@ struct dpm2d_batch {
     return a;
   }
 
+  // One launch of the step over a's cells, whose rings have at most maxnv_k
+  // vertices: the team kernel when it is chosen and applies, else one warp
+  // per cell.
+  cudaError_t launch_one(const Step2DArgs &a, int maxnv_k, cudaStream_t s) const {
+    if (team && !att && maxnv_k <= 64)
+      return maxnv_k <= 32 ? launch_team2d_s1(a, occ, s) : launch_team2d_s2(a, occ, s);
+    return launch_step2d(a, maxnv_k, warps, variant(), s);
+  }
+
   // One step of every cell: a single launch, or one launch per vertex-slot
   // class (by the tissue's largest ring), the largest rings first on the
   // auxiliary stream and the smallest on `s`, joined back into `s`.  The
   // classes write disjoint cells and read only the step's inputs, so their
   // order does not matter.
   cudaError_t launch_step(const Step2DArgs &a0, cudaStream_t s) {
-    if (serving || nclass <= 1) return launch_step2d(a0, maxnv, warps, variant(), s);
+    if (serving) return launch_step2d(a0, maxnv, warps, variant(), s);
+    if (nclass <= 1) return launch_one(a0, maxnv, s);
     cudaError_t e = cudaEventRecord(ev_fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev_fork, 0);
     int first = 0;
@@ -239,7 +250,7 @@ struct dpm2d_batch {
       a.order = d_order + class_begin[k];
       a.ncells = n;
       a.sched = d_sched + 2 * k;
-      e = launch_step2d(a, 32 << k, warps, variant(), k == first ? s : aux);
+      e = launch_one(a, 32 << k, k == first ? s : aux);
     }
     if (e == cudaSuccess) e = cudaEventRecord(ev_join, aux);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
@@ -645,9 +656,11 @@ int dpm2d_set_tuning(dpm2d_batch *b, int rebuild_period, float skin_rel, int war
 
 int dpm2d_set_kernel_variant(dpm2d_batch *b, int variant) {
   if (int r = check_batch(b)) return r;
-  if (variant < 0 || (variant & ~11) != 0)
-    return fail(DPM_EINVAL, "step-kernel variant must be 0..3, plus 8 to switch off the resident run");
+  if (variant < 0 || (variant & ~(3 | 8 | kStepVariantTeam)) != 0)
+    return fail(DPM_EINVAL, "step-kernel variant must be 0..3, plus 8 to switch off the resident "
+                            "run and 32 for four warps per cell");
   b->occ = variant & 3;
+  b->team = (variant & kStepVariantTeam) != 0;
   b->no_resident = (variant & 8) != 0;
   b->clear_graphs();
   return DPM_OK;
@@ -980,7 +993,7 @@ std::string tune_key(const dpm2d_batch *b, int sm_count) {
   };
   char buf[160];
   // "k2": step-kernel variants 0..3 (register cap x dynamic schedule)
-  std::snprintf(buf, sizeof(buf), "2d k2 sm%d t%d c%d v%d nv%d", sm_count, bucket(b->ntissues),
+  std::snprintf(buf, sizeof(buf), "2d k3 sm%d t%d c%d v%d nv%d", sm_count, bucket(b->ntissues),
                 bucket(b->ncells), bucket(b->nverts), b->maxnv);
   return buf;
 }
@@ -1041,7 +1054,8 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache, in
   float sk = 0.0f, best_ms = -1.0f;
   auto apply = [&](int ww, int oo, int pp, float ss) -> int {
     b->warps = ww;
-    b->occ = oo;
+    b->occ = oo & 3;
+    b->team = (oo & kStepVariantTeam) != 0;
     b->rebuild_period = pp;
     b->skin_rel = ss;
     b->clear_graphs();
@@ -1080,12 +1094,17 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache, in
     const int warps_set[3] = {4, 8, 16};
     const int periods[3] = {8, 16, 32};
     const float skins[3] = {0.08f, 0.15f, 0.3f};
+    // step-kernel variants: register cap x schedule, and (no attraction,
+    // rings of at most 64) four warps per cell with or without the cap
+    const int vars[6] = {0, 1, 2, 3, kStepVariantTeam, kStepVariantTeam | 1};
+    const int nvar = (!b->att && b->maxnv <= 64) ? 6 : 4;
     int rc = DPM_OK;
     for (int wi = 0; wi < 3 && rc == DPM_OK; ++wi)
-      for (int oi = 0; oi < 4 && rc == DPM_OK; ++oi)
+      for (int oi = 0; oi < nvar && rc == DPM_OK; ++oi)
         for (int pi = 0; pi < 3 && rc == DPM_OK; ++pi) {
           if (warps_set[wi] == 16 && b->maxnv > 128) continue;
-          if ((rc = apply(warps_set[wi], oi, periods[pi], skins[pi]))) break;
+          if ((vars[oi] & kStepVariantTeam) && warps_set[wi] != 8) continue;
+          if ((rc = apply(warps_set[wi], vars[oi], periods[pi], skins[pi]))) break;
           cudaError_t e = restore();
           if (e != cudaSuccess) {
             rc = cuda_fail(e, "tuner restore");
@@ -1107,7 +1126,7 @@ int dpm2d_autotune(dpm2d_batch *b, float dt, int trial_blocks, int use_cache, in
           if (best_ms < 0.0f || ms < best_ms) {
             best_ms = ms;
             w = warps_set[wi];
-            o = oi;
+            o = vars[oi];
             p = periods[pi];
             sk = skins[pi];
           }

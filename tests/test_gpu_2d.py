@@ -243,7 +243,7 @@ def test_kernel_variants_identical(ctx):
                             phi=float(rng.uniform(0.6, 0.9)), Kb=0.01, seed=200 + t)
               for t in range(5)]
     out = {}
-    for variant in (0, 1, 2, 3, 8, 11):
+    for variant in (0, 1, 2, 3, 8, 11, 40, 41):
         for warps in (4, 8, 16):
             b = gpu_batch2d(ctx, states, dict(warps=warps))
             b.set_kernel_variant(variant)
@@ -253,6 +253,35 @@ def test_kernel_variants_identical(ctx):
     ref = out[(1, 8)]
     for k, (xy, F) in out.items():
         assert np.array_equal(xy, ref[0]) and np.array_equal(F, ref[1]), k
+
+
+def test_team_cells_same_bits(ctx):
+    """Four warps per cell (variant bit 5; no attraction): the warps split a
+    cell's listed neighbours and OR their containment flags, which is the
+    one-warp result bit for bit -- positions, forces and flags -- for rings
+    of one and two slots in one batch, and the oracle's."""
+    rng = np.random.default_rng(47)
+    states = [make_tissue2d(150, 32, r0=rng.permutation(np.r_[np.ones(75), np.full(75, 1.4)]),
+                            calA=rng.uniform(1.0, 1.2, 150), Kb=0.01, phi=0.85, seed=320),
+              make_tissue2d(90, rng.choice([20, 48], size=90), calA=1.1, phi=0.8, seed=321),
+              make_tissue2d(70, 16, phi=0.9, seed=322)]
+    res = []
+    for variant in (11, 40, 41):
+        b = gpu_batch2d(ctx, states)
+        b.set_kernel_variant(variant)
+        b.step(40, DT)
+        xy, F = b.download()
+        res.append((xy, F, b.contained()))
+    for r in res[1:]:
+        assert all(np.array_equal(u, v) for u, v in zip(res[0], r))
+    s = perturb(states[0], 0.05, 3)
+    b = gpu_batch2d(ctx, [s])
+    b.set_kernel_variant(41)
+    b.step(1, DT)
+    _, F = b.download()
+    _, rF, rflags = oracle_run(s, 1)
+    assert np.array_equal(b.contained(), rflags)
+    assert rel_norm_err(F, rF) <= F_TOL
 
 
 def test_resident_run_same_bits(ctx):
