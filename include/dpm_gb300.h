@@ -272,6 +272,12 @@ int dpm3d_sizes(dpm3d_batch *b, int *ncells, long *nvertices);
 /* Neighbour-list rebuild period (steps) and skin relative to the mean cell
  * diameter (0 keeps the current value). */
 int dpm3d_set_tuning(dpm3d_batch *b, int rebuild_period, float skin_rel);
+/* Threads per cell of the step kernel: 128, 256 or 512, or 0 for the
+ * default (256 when the batch has more cells than two 512-thread blocks per
+ * SM hold and the mesh's shared memory lets four cells share an SM, e.g.
+ * subdivision 2; 512 otherwise).  Results are the same bits for every
+ * choice. */
+int dpm3d_set_block_threads(dpm3d_batch *b, int threads);
 /* Per-vertex count of other cells whose winding number passed the
  * reference's threshold in the last step (uint8 per vertex). */
 int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts);

@@ -63,6 +63,7 @@ SIGNATURES = {
     "dpm3d_sizes": (ctypes.c_int, [_vp, _c_int_p, _c_long_p]),
     "dpm3d_last_winding": (ctypes.c_int, [_vp, _c_ubyte_p]),
     "dpm3d_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_float]),
+    "dpm3d_set_block_threads": (ctypes.c_int, [_vp, ctypes.c_int]),
     "dpm2d_step_noalloc": (ctypes.c_int, [ctypes.c_int, _c_uint_p] + [_c_float_p] * 6 +
                            [ctypes.c_float] * 3 + [ctypes.c_int, _vp, _vp, ctypes.c_int,
                                                    ctypes.c_float, _vp]),
@@ -419,6 +420,10 @@ class Batch3D:
 
     def set_tuning(self, rebuild_period=0, skin_rel=0.0):
         check(self.lib.dpm3d_set_tuning(self.h, rebuild_period, skin_rel))
+
+    def set_block_threads(self, threads: int = 0):
+        """Threads per cell of the step kernel (128, 256, 512; 0: default)."""
+        check(self.lib.dpm3d_set_block_threads(self.h, threads))
 
     def upload(self, xyz):
         xyz = _f32(xyz)

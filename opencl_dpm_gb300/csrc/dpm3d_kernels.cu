@@ -32,11 +32,17 @@ namespace dpm {
 
 namespace {
 
-// 16 warps per cell: the winding candidates of a cell (one warp each) are
-// the bulk of the work, and a few hundred cells must fill 152 SMs
-// (measured on the 256-cell monolayer: 512 threads 27% faster than 256).
+// Threads per cell of k3d_step (NT): 512 (16 warps) by default -- the
+// winding candidates of a cell (one warp each) are the bulk of the work, and
+// a few hundred cells must fill 152 SMs (measured on the 256-cell monolayer
+// at subdivision 3: 512 threads 27% faster than 256); meshes whose shared
+// memory lets four or eight cells share an SM take 256 or 128 threads.
+// Every block-wide sum is formed in the order of a 512-thread block
+// (block_sum_v), so the block size changes no bit of the results.
+// k3d_geom and k3d_diag run 512 threads.
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
+constexpr int kSumThreads = 512;
 constexpr unsigned kFull = 0xffffffffu;
 
 struct f3 {
@@ -58,34 +64,47 @@ __device__ __forceinline__ f3 normalize(f3 a) {
   return a / sqrtf(l2);
 }
 
-__device__ float block_sum(float v, float *red) {
-  v = warp_sum(v);
+// Block sum of per-thread partials, added as a kSumThreads-thread block
+// adds them: v[r] is the partial of virtual thread threadIdx.x + r * NT (a
+// block of NT threads runs kSumThreads / NT virtual threads per thread);
+// the 32 virtual threads of a virtual warp are summed by the warp's
+// butterfly, then the virtual warps' sums in order.
+template <int NT>
+__device__ float block_sum_v(const float (&v)[kSumThreads / NT], float *red) {
+  constexpr int R = kSumThreads / NT;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float ws[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) ws[r] = warp_sum(v[r]);
   __syncthreads();
-  if (lane == 0) red[w] = v;
+  if (lane == 0) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) red[w + r * (NT / 32)] = ws[r];
+  }
   __syncthreads();
-  float r = 0.0f;
-  for (int i = 0; i < kWarps; ++i) r += red[i];
-  return r;
+  float t = 0.0f;
+  for (int i = 0; i < kSumThreads / 32; ++i) t += red[i];
+  return t;
 }
-__device__ float block_max(float v, float *red) {
+template <int NT> __device__ float block_max(float v, float *red) {
   v = warp_max(v);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) red[w] = v;
   __syncthreads();
   float r = -INFINITY;
-  for (int i = 0; i < kWarps; ++i) r = fmaxf(r, red[i]);
+  for (int i = 0; i < NT / 32; ++i) r = fmaxf(r, red[i]);
   return r;
 }
 
 // Centre of mass (sum times 1/NV, Cell3D_Kernel.cl:35-44), bounding radius
 // and longest edge of the mesh held in shared memory.
-template <typename FaceIdx>
+template <int NT, typename FaceIdx>
 __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, int nv,
                             const FaceIdx *faces, int nf, float *red) {
+  constexpr int R = kSumThreads / NT;
   float e2 = 0.f;
-  for (int f = threadIdx.x; f < nf; f += kThreads) {
+  for (int f = threadIdx.x; f < nf; f += NT) {
     const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
     const int a[3] = {i0, i1, i2}, b[3] = {i1, i2, i0};
 #pragma unroll
@@ -94,24 +113,28 @@ __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, i
       e2 = fmaxf(e2, dx * dx + dy * dy + dz * dz);
     }
   }
-  const float emax = sqrtf(block_max(e2, red));
-  float sx = 0.f, sy = 0.f, sz = 0.f;
-  for (int v = threadIdx.x; v < nv; v += kThreads) {
-    sx += px[v];
-    sy += py[v];
-    sz += pz[v];
+  const float emax = sqrtf(block_max<NT>(e2, red));
+  float sx[R], sy[R], sz[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    sx[r] = sy[r] = sz[r] = 0.f;
+    for (int v = threadIdx.x + r * NT; v < nv; v += kSumThreads) {
+      sx[r] += px[v];
+      sy[r] += py[v];
+      sz[r] += pz[v];
+    }
   }
   const float inv = 1.0f / (float)nv;
   Geom3D g;
-  g.cx = block_sum(sx, red) * inv;
-  g.cy = block_sum(sy, red) * inv;
-  g.cz = block_sum(sz, red) * inv;
+  g.cx = block_sum_v<NT>(sx, red) * inv;
+  g.cy = block_sum_v<NT>(sy, red) * inv;
+  g.cz = block_sum_v<NT>(sz, red) * inv;
   float r2 = 0.f;
-  for (int v = threadIdx.x; v < nv; v += kThreads) {
+  for (int v = threadIdx.x; v < nv; v += NT) {
     const float dx = px[v] - g.cx, dy = py[v] - g.cy, dz = pz[v] - g.cz;
     r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
   }
-  g.R = sqrtf(block_max(r2, red));
+  g.R = sqrtf(block_max<NT>(r2, red));
   g.emax = emax;
   // Inner ball.  With the centre as origin, face (a, b, c) has the triple
   // product t = a.(b x c), whose sign is the sign of the reference's face
@@ -120,27 +143,32 @@ __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, i
   // angles sum to less than 8 pi (each is at most area / plane distance^2),
   // the mesh winds exactly once around the centre, and no face comes closer
   // than the smallest plane distance, so the same holds in that ball.
-  float dmin = INFINITY, bound = 0.f, npos = 0.f;
-  for (int f = threadIdx.x; f < nf; f += kThreads) {
-    const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
-    const f3 a = mk(px[i0] - g.cx, py[i0] - g.cy, pz[i0] - g.cz);
-    const f3 b = mk(px[i1] - g.cx, py[i1] - g.cy, pz[i1] - g.cz);
-    const f3 c = mk(px[i2] - g.cx, py[i2] - g.cy, pz[i2] - g.cz);
-    const f3 n = cross(b - a, c - a);
-    const float nl = sqrtf(dot(n, n));
-    const float t = dot(a, cross(b, c));
-    const float d = fabsf(t) / nl;  // NaN or 0 for a degenerate face
-    dmin = d > 0.0f ? fminf(dmin, d) : -1.0f;
-    bound += 0.5f * nl / (d * d);
-    npos += t > 0.0f ? 1.0f : 0.0f;
+  // (dmin is -1 once any face is degenerate, whatever the order.)
+  float dmin = INFINITY, bound[R], npos[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    bound[r] = npos[r] = 0.f;
+    for (int f = threadIdx.x + r * NT; f < nf; f += kSumThreads) {
+      const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
+      const f3 a = mk(px[i0] - g.cx, py[i0] - g.cy, pz[i0] - g.cz);
+      const f3 b = mk(px[i1] - g.cx, py[i1] - g.cy, pz[i1] - g.cz);
+      const f3 c = mk(px[i2] - g.cx, py[i2] - g.cy, pz[i2] - g.cz);
+      const f3 n = cross(b - a, c - a);
+      const float nl = sqrtf(dot(n, n));
+      const float t = dot(a, cross(b, c));
+      const float d = fabsf(t) / nl;  // NaN or 0 for a degenerate face
+      dmin = d > 0.0f ? fminf(dmin, d) : -1.0f;
+      bound[r] += 0.5f * nl / (d * d);
+      npos[r] += t > 0.0f ? 1.0f : 0.0f;
+    }
   }
-  dmin = -block_max(-dmin, red);
-  bound = block_sum(bound, red);
-  npos = block_sum(npos, red);
-  const bool one_sign = npos == (float)nf || npos == 0.0f;
-  const bool ok = one_sign && dmin > 0.0f && bound < 8.0f * (float)M_PI * 0.999f;
+  dmin = -block_max<NT>(-dmin, red);
+  const float bsum = block_sum_v<NT>(bound, red);
+  const float ns = block_sum_v<NT>(npos, red);
+  const bool one_sign = ns == (float)nf || ns == 0.0f;
+  const bool ok = one_sign && dmin > 0.0f && bsum < 8.0f * (float)M_PI * 0.999f;
   g.rin = ok ? dmin * (1.0f - 1e-4f) : 0.0f;
-  g.wind = npos == (float)nf ? 1.0f : -1.0f;
+  g.wind = ns == (float)nf ? 1.0f : -1.0f;
   g.pad0 = 0.0f;
   return g;
 }
@@ -183,6 +211,7 @@ __host__ __device__ __forceinline__ int q_region(int nv, int nf, int ne) {
   return a > b ? a : b;
 }
 
+template <int NT>
 __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool bend) {
   Smem3D s;
   s.pb = reinterpret_cast<float4 *>(base);
@@ -207,7 +236,7 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool
   f += q_region(nv, nf, ne);
   s.red = f; f += 64;
   s.near = reinterpret_cast<unsigned *>(f);
-  f += kWarps * kNearWords;
+  f += (NT / 32) * kNearWords;
   if (bend) {
     s.bnx = f; f += nf;
     s.bny = f; f += nf;
@@ -231,7 +260,7 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool
   s.pvert = h;
   h += nv;
   s.nlist = h;
-  h += kWarps * kNearList;
+  h += (NT / 32) * kNearList;
   s.defer = h;
   h += kDefer;
   s.wnc = reinterpret_cast<unsigned char *>(h);
@@ -518,16 +547,17 @@ __device__ __forceinline__ float winding_at(const Smem3D &s, const Mesh3D &m, in
 // Stages cell j's vertices, shifted to the periodic image nearest this cell,
 // into s.q*, and the bounding spheres of its patches, from the same shifted
 // coordinates, into s.pb (the whole block; no barrier).
+template <int NT>
 __device__ __forceinline__ void stage_neighbour(const Smem3D &s, const Step3DArgs &a, int j,
                                                 f3 shift, int NV, int NP, int tid, int w,
                                                 int lane) {
   const size_t bj = (size_t)j * NV;
-  for (int k = tid; k < NV; k += kThreads) {
+  for (int k = tid; k < NV; k += NT) {
     s.qx[k] = a.xin[bj + k] + shift.x;
     s.qy[k] = a.yin[bj + k] + shift.y;
     s.qz[k] = a.zin[bj + k] + shift.z;
   }
-  for (int p = w; p < NP; p += kWarps) {
+  for (int p = w; p < NP; p += NT / 32) {
     const int o = s.poff[p], n = s.poff[p + 1] - o;
     f3 q = mk(0.f, 0.f, 0.f);
     if (lane < n) {
@@ -583,12 +613,14 @@ __device__ __forceinline__ void attract_pair(f3 p, f3 q, float L0i, float L0j, f
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k3d_step(Step3DArgs a) {
+  constexpr int kW = NT / 32;  // warps per cell
   extern __shared__ __align__(16) char smem3d[];
   const int c = blockIdx.x;
   const int NV = a.mesh.nv, NF = a.mesh.nf;
   const bool bend_any = a.bend != 0;
-  Smem3D s = carve(smem3d, NV, NF, a.mesh.ne, bend_any);
+  Smem3D s = carve<NT>(smem3d, NV, NF, a.mesh.ne, bend_any);
   const Cell3D P = a.cells[c];
   if (!P.active) return;  // an empty slot (uniform over the block)
   const Tissue3D T = a.tissues[P.tissue];
@@ -596,7 +628,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   if (a.step_index >= T.run_now) {
     // the tissue's step budget is spent: carry its state over unchanged
-    for (int v = tid; v < NV; v += kThreads) {
+    for (int v = tid; v < NV; v += NT) {
       a.xout[base + v] = a.xin[base + v];
       a.yout[base + v] = a.yin[base + v];
       a.zout[base + v] = a.zin[base + v];
@@ -607,15 +639,15 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   const bool write_out =
       a.all_forces != 0 || (a.step_index == T.run_now - 1 && T.steps_left == 0);
 
-  for (int v = tid; v < NV; v += kThreads) {
+  for (int v = tid; v < NV; v += NT) {
     s.px[v] = a.xin[base + v];
     s.py[v] = a.yin[base + v];
     s.pz[v] = a.zin[base + v];
     s.wnc[v] = 0;
   }
-  for (int i = tid; i < 3 * NF; i += kThreads) s.faces[i] = a.mesh.faces[i];
+  for (int i = tid; i < 3 * NF; i += NT) s.faces[i] = a.mesh.faces[i];
   const int NP = a.mesh.np;
-  for (int i = tid; i < NV; i += kThreads) s.pvert[i] = a.mesh.pvert[i];
+  for (int i = tid; i < NV; i += NT) s.pvert[i] = a.mesh.pvert[i];
   if (tid <= NP) s.poff[tid] = a.mesh.poff[tid];
   if (tid < 3) s.ncand[tid] = 0;
   __syncthreads();
@@ -624,19 +656,23 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   const f3 C = mk(gi.cx, gi.cy, gi.cz);
 
   // volume (getVolume, Cell3D_Kernel.cl:46-64)
-  float vpart = 0.0f;
-  for (int f = tid; f < NF; f += kThreads) {
-    const f3 P0 = vtx(s, s.faces[3 * f]), P1 = vtx(s, s.faces[3 * f + 1]),
-             P2 = vtx(s, s.faces[3 * f + 2]);
-    vpart += dot(cross(P0, P1), P2) / 6.0f;
+  float vpart[kSumThreads / NT];
+#pragma unroll
+  for (int r = 0; r < kSumThreads / NT; ++r) {
+    vpart[r] = 0.0f;
+    for (int f = tid + r * NT; f < NF; f += kSumThreads) {
+      const f3 P0 = vtx(s, s.faces[3 * f]), P1 = vtx(s, s.faces[3 * f + 1]),
+               P2 = vtx(s, s.faces[3 * f + 2]);
+      vpart[r] += dot(cross(P0, P1), P2) / 6.0f;
+    }
   }
-  const float volume = fabsf(block_sum(vpart, s.red));
+  const float volume = fabsf(block_sum_v<NT>(vpart, s.red));
   const float kvol = -P.Kv * (volume / P.v0 - 1.0f);
 
   // edge pass of SurfaceAreaForceUpdate: every face term uses the unit
   // vector and length of its edges, formed here once per edge
   if (!(P.Ka < 1e-8f)) {
-    for (int e = tid; e < a.mesh.ne; e += kThreads) {
+    for (int e = tid; e < a.mesh.ne; e += NT) {
       const f3 lv = vtx(s, a.mesh.eva[2 * e + 1]) - vtx(s, a.mesh.eva[2 * e]);
       const float L = sqrtf(dot(lv, lv));
       const f3 n = lv / L;
@@ -649,7 +685,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   // triangle bending, face pass (extension): unit normals, then G per face
   const bool bend = bend_any && P.Kb != 0.0f;
   if (bend) {
-    for (int f = tid; f < NF; f += kThreads) {
+    for (int f = tid; f < NF; f += NT) {
       const f3 p0 = vtx(s, s.faces[3 * f]), p1 = vtx(s, s.faces[3 * f + 1]),
                p2 = vtx(s, s.faces[3 * f + 2]);
       const f3 n = cross(p1 - p0, p2 - p0);
@@ -663,7 +699,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   }
   __syncthreads();
   if (bend) {
-    for (int f = tid; f < NF; f += kThreads) {
+    for (int f = tid; f < NF; f += NT) {
       f3 G = mk(0.f, 0.f, 0.f);
       const float l = s.bnl[f];
       if (l != 0.0f) {
@@ -685,7 +721,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
 
   // per-vertex shape forces, in the reference's accumulation order
   const float range = P.adh;
-  for (int v = tid; v < NV; v += kThreads) {
+  for (int v = tid; v < NV; v += NT) {
     f3 F = mk(0.f, 0.f, 0.f);
     const int e0 = a.mesh.inc_off[v], e1 = a.mesh.inc_off[v + 1];
     // VolumeForceUpdate (Cell3D_Kernel.cl:95-111)
@@ -785,18 +821,18 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
       // when nobody reads it.
       int *cnt = s.ncand + par;
       const float rj = reach * (1.0f + 1e-4f) + 1e-5f * mag;
-      for (int v = tid; v < NV; v += kThreads) {
+      for (int v = tid; v < NV; v += NT) {
         const f3 d = vtx(s, v) - cj;
         if (dot(d, d) <= rj * rj) s.cand[atomicAdd(cnt, 1)] = (uint16_t)v;
       }
-      stage_neighbour(s, a, j, shift, NV, NP, tid, w, lane);
+      stage_neighbour<NT>(s, a, j, shift, NV, NP, tid, w, lane);
       __syncthreads();
       const int ncand = *cnt;
       if (tid == 0) s.ncand[par ^ 1] = 0;
       par ^= 1;
       if (ncand > 0) {
         unsigned *nearm = s.near + w * kNearWords;
-        for (int i = w; i < ncand; i += kWarps) {
+        for (int i = w; i < ncand; i += kW) {
           const int v = s.cand[i];
           const f3 pt = vtx(s, v);
           bool deferred;
@@ -828,14 +864,14 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
         float *tb = s.terms + (d & 1) * NF;
         const int v = s.defer[d];
         const f3 pt = vtx(s, v);
-        for (int f = tid; f < NF; f += kThreads) {
+        for (int f = tid; f < NF; f += NT) {
           float num, denom;
           face_term(s, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num, denom);
           tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
         }
         __syncthreads();
         if (tid == 0 && d == nd - 1) s.ncand[2] = 0;
-        if (w == d % kWarps) {
+        if (w == d % kW) {
           float part = 0.0f;
           for (int f = lane; f < NF; f += 32) part += tb[f];
           const float wn = warp_sum(part) / (4.0f * (float)M_PI);
@@ -880,11 +916,11 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
       const bool prune = !T.pbc || (fabsf(dc.x) + ext < 0.49f * L &&
                                     fabsf(dc.y) + ext < 0.49f * L &&
                                     fabsf(dc.z) + ext < 0.49f * L);
-      stage_neighbour(s, a, j, shift, NV, NP, tid, w, lane);
+      stage_neighbour<NT>(s, a, j, shift, NV, NP, tid, w, lane);
       __syncthreads();
       const size_t bj = (size_t)j * NV;
       const float range2 = range * range;
-      for (int v = tid; v < NV; v += kThreads) {
+      for (int v = tid; v < NV; v += NT) {
         const f3 p = vtx(s, v);
         const f3 d0 = p - cj;
         const float rj = gj.R * (1.0f + 1e-4f) + range;
@@ -917,7 +953,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
   }
 
   // EulerPosition (Cell3D_Kernel.cl:371-381) and outputs
-  for (int v = tid; v < NV; v += kThreads) {
+  for (int v = tid; v < NV; v += NT) {
     const float nx = __fadd_rn(s.px[v], __fmul_rn(s.fx[v], a.dt));
     const float ny = __fadd_rn(s.py[v], __fmul_rn(s.fy[v], a.dt));
     const float nz = __fadd_rn(s.pz[v], __fmul_rn(s.fz[v], a.dt));
@@ -935,7 +971,7 @@ __global__ void __launch_bounds__(kThreads, 2) k3d_step(Step3DArgs a) {
     s.pz[v] = nz;
   }
   __syncthreads();
-  const Geom3D g = mesh_geom(s.px, s.py, s.pz, NV, s.faces, NF, s.red);
+  const Geom3D g = mesh_geom<NT>(s.px, s.py, s.pz, NV, s.faces, NF, s.red);
   if (tid == 0) {
     a.geom_out[c] = g;
     if (!(isfinite(g.cx) && isfinite(g.cy) && isfinite(g.cz) && isfinite(g.R)))
@@ -962,7 +998,7 @@ __global__ void __launch_bounds__(kThreads)
     pz[v] = z[base + v];
   }
   __syncthreads();
-  const Geom3D g = mesh_geom(px, py, pz, nv, faces, nf, red);
+  const Geom3D g = mesh_geom<kThreads>(px, py, pz, nv, faces, nf, red);
   if (threadIdx.x == 0) geom[blockIdx.x] = g;
 }
 
@@ -1228,34 +1264,58 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
 
 } // namespace
 
-size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend) {
-  size_t floats = (size_t)6 * nv + (size_t)q_region(nv, nf, ne) + 64 +
-                  (size_t)kWarps * kNearWords + (bend ? (size_t)7 * nf : 0) + 4 +
-                  kMaxPatches3D + 4;
-  size_t halves = (size_t)3 * nf + 2 * (size_t)nv + (size_t)kWarps * kNearList + kDefer;
+size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend, int threads) {
+  const size_t warps = (size_t)threads / 32;
+  size_t floats = (size_t)6 * nv + (size_t)q_region(nv, nf, ne) + 64 + warps * kNearWords +
+                  (bend ? (size_t)7 * nf : 0) + 4 + kMaxPatches3D + 4;
+  size_t halves = (size_t)3 * nf + 2 * (size_t)nv + warps * kNearList + kDefer;
   return sizeof(float4) * kMaxPatches3D + floats * 4 + halves * 2 + (size_t)nv + 16;
 }
 
-// The kernel's dynamic shared-memory limit is a per-device attribute shared
+int step3d_threads(int nv, int nf, int ne, bool bend, int ncells, int sm_count) {
+  // A cell's step is latency-bound: while two 512-thread blocks per SM hold
+  // every cell, 16 warps per cell finish soonest; with more cells, 256
+  // threads let four cells share an SM when their shared memory fits in its
+  // 228 KB (1 KB reserved per block).  Measured on subdivision-2 batches of
+  // 1,660-2,048 cells: 256 threads 14-17% faster; on 64-256 cells, or at
+  // subdivision 3 (96 KB per block), 512 faster.
+  const size_t b256 = step3d_smem_bytes(nv, nf, ne, bend, 256) + 1024;
+  const bool four_fit = 4 * b256 <= (size_t)228 * 1024;
+  return four_fit && ncells > 2 * sm_count ? 256 : 512;
+}
+
+// The kernels' dynamic shared-memory limit is a per-device attribute shared
 // by every batch: it is only ever raised, so a batch of a smaller mesh made
 // after a larger one does not lower it under the larger one's launches.
 cudaError_t prepare_step3d(int nv, int nf, int ne, bool bend) {
   static std::mutex mu;
   static size_t granted[64] = {0};
-  const size_t bytes = step3d_smem_bytes(nv, nf, ne, bend);
+  // the 512-thread block needs the most; the smaller ones get the same limit
+  const size_t bytes = step3d_smem_bytes(nv, nf, ne, bend, 512);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(mu);
   if (dev >= 0 && dev < 64 && bytes <= granted[dev]) return cudaSuccess;
-  e = cudaFuncSetAttribute(k3d_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  e = cudaFuncSetAttribute(k3d_step<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k3d_step<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k3d_step<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes);
   if (e == cudaSuccess && dev >= 0 && dev < 64) granted[dev] = bytes;
   return e;
 }
 
-cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s) {
-  const size_t bytes = step3d_smem_bytes(a.mesh.nv, a.mesh.nf, a.mesh.ne, a.bend != 0);
-  k3d_step<<<a.ncells, kThreads, bytes, s>>>(a);
+cudaError_t launch_step3d(const Step3DArgs &a, int threads, cudaStream_t s) {
+  const size_t bytes = step3d_smem_bytes(a.mesh.nv, a.mesh.nf, a.mesh.ne, a.bend != 0, threads);
+  switch (threads) {
+    case 128: k3d_step<128><<<a.ncells, 128, bytes, s>>>(a); break;
+    case 256: k3d_step<256><<<a.ncells, 256, bytes, s>>>(a); break;
+    case 512: k3d_step<512><<<a.ncells, 512, bytes, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

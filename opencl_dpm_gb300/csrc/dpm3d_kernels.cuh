@@ -67,8 +67,15 @@ cudaError_t launch_diag3d(const float *x, const float *y, const float *z, const 
                           const Cell3D *cells, double *out, int ncells, cudaStream_t s);
 cudaError_t launch_binprep3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
 cudaError_t launch_neighbors3d(const Rebuild3DArgs &a, int local_bits, cudaStream_t s);
-size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend);
+// Dynamic shared memory of one k3d_step block of `threads` threads.
+size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend, int threads);
+// Threads per cell the runtime picks: 256 when a launch has more cells than
+// two 512-thread blocks per SM hold and four 256-thread blocks' shared memory
+// fits on an SM, else 512.
+int step3d_threads(int nv, int nf, int ne, bool bend, int ncells, int sm_count);
 cudaError_t prepare_step3d(int nv, int nf, int ne, bool bend);
-cudaError_t launch_step3d(const Step3DArgs &a, cudaStream_t s);
+// One fused 3D step, one block of `threads` (128, 256 or 512) per cell; every
+// block size gives the same bits.
+cudaError_t launch_step3d(const Step3DArgs &a, int threads, cudaStream_t s);
 
 } // namespace dpm

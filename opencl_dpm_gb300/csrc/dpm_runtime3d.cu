@@ -123,6 +123,7 @@ struct dpm3d_batch {
   int local_bits = 1, key_bits = 1;
   int rebuild_period = 8;
   float skin_rel = 0.1f;
+  int threads = 0;  // threads per cell of the step (0: step3d_threads's choice)
   // slot pools: launches cover the tissues [0, run_tissues) and their cells
   // [0, run_cells) only (0: all)
   int run_tissues = 0, run_cells = 0;
@@ -219,9 +220,11 @@ struct dpm3d_batch {
   cudaError_t enqueue_block(int len, int from, float dt, bool last, cudaStream_t s) {
     cudaError_t e = enqueue_rebuild(from, len, s);
     if (e != cudaSuccess) return e;
+    const int nt =
+        threads ? threads : step3d_threads(nv, nf, mesh.ne, bend, nc(), ctx->sm_count);
     int f = from;
     for (int i = 0; i < len; ++i) {
-      e = launch_step3d(step_args(f, dt, last && i == len - 1, i), s);
+      e = launch_step3d(step_args(f, dt, last && i == len - 1, i), nt, s);
       if (e != cudaSuccess) return e;
       f = 1 - f;
     }
@@ -750,6 +753,15 @@ int dpm3d_last_winding(dpm3d_batch *b, unsigned char *counts) {
   DPM_CUDA_TRY(cudaMemcpyAsync(counts, b->d_wn, b->nverts, cudaMemcpyDeviceToHost,
                                b->stream));
   DPM_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DPM_OK;
+}
+
+int dpm3d_set_block_threads(dpm3d_batch *b, int threads) {
+  if (int r = check3(b)) return r;
+  if (threads != 0 && threads != 128 && threads != 256 && threads != 512)
+    return fail(DPM_EINVAL, "threads per cell must be 0, 128, 256 or 512");
+  b->threads = threads;
+  b->clear_graphs();
   return DPM_OK;
 }
 

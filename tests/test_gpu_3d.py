@@ -150,6 +150,38 @@ def test_monolayer_level3_contacts(ctx):
             assert rel_norm_err(F, rF) <= F_TOL
 
 
+@pytest.mark.parametrize("level", [2, 3])
+def test_block_sizes_same_bits(ctx, level):
+    """128, 256 and 512 threads per cell (and the default) give the same
+    bits: every block-wide sum is formed in the 512-thread order.  A
+    contact-rich monolayer with bending and adhesion, and the opt-in
+    attraction."""
+    import bench
+    from opencl_dpm_gb300 import clDPM
+    from oracle.oracle import Tissue3DState
+    t = bench.build_monolayer(clDPM, np.random.default_rng(21), 12, level)
+    s = Tissue3DState(nv=t["nv"], faces=t["faces"], xyz=t["xyz"].copy(), Kv=t["Kv"], Ka=t["Ka"],
+                      Ks=t["Ks"], v0=t["v0"], a0=t["a0"], l0=t["l0"], L=float(t["L"]), Kre=1.0,
+                      pbc=1, Kb=t["Kb"], adh=t["adh"])
+    for kat in (0.0, 0.05):
+        s.Kat = kat
+        out = {}
+        for threads in (512, 256, 128, 0):
+            b = gpu_batch3d(ctx, [s])
+            b.set_block_threads(threads)
+            b.step(10, DT)
+            x, F = b.download()
+            out[threads] = (x, F, b.winding())
+        x0, F0, w0 = out[512]
+        assert w0.sum() > 0
+        for threads in (256, 128, 0):
+            x, F, w = out[threads]
+            assert np.array_equal(x, x0) and np.array_equal(F, F0), (kat, threads)
+            assert np.array_equal(w, w0), (kat, threads)
+    with pytest.raises(Exception):
+        b.set_block_threads(384)
+
+
 def test_larger_mesh_after_smaller(ctx):
     """A batch of a larger mesh still steps after a batch of a smaller mesh
     was made (the step's shared-memory limit is shared by all batches)."""
