@@ -20,7 +20,9 @@ time.
 
 Also reported (keys of the same line): the plain single-system paths -- the
 1,024-cell compression protocol ("plain"), the 16-cell run of 10,000 steps
-("plain_c0"), the 256-cell 3D monolayer ("plain3d") -- 48 monolayers in one
+("plain_c0"), the 256-cell 3D monolayer ("plain3d") -- the sweep's own
+tissues run one after another through the plain path ("sequential"; the
+same for the 3D batch and for the served requests), 48 monolayers in one
 batch ("batched3d"), the same 32-tissue sample the reference arm times
 ("same_sample"), the sweep's full 20,000-step run ("steady_state"), the
 reference's dispersion on the device ("disperse"), the dominant kernel's HBM
@@ -461,12 +463,17 @@ def run_ours(args, rank, world, local_rank):
     p3 = plain3d(ctx, timed, max(3, args.steps))
     b3 = batched3d(ctx, timed, max(3, args.steps))
     b3["batched_over_plain"] = round(b3["value"] / p3["value"], 2)
+    seq2 = sequential_2d(ctx, timed, tissues)
+    seq3 = sequential_3d(ctx, timed, workload_batched3d())
+    b3["sequential"] = seq3
+    b3["batched_over_sequential"] = round(b3["value"] / seq3["value"], 2)
     steady = steady_state_leg(ctx, timed, geo)
     disp = disperse_leg(ctx, tissues, geo)
 
     served = None
     if args.serve_requests > 0:
-        served = run_served(ctx, args.serve_requests, plain2d=c1["value"], plain3d=p3["value"])
+        served = run_served(ctx, timed, args.serve_requests, plain2d=c1["value"],
+                            plain3d=p3["value"])
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -481,6 +488,8 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "e2e": e2e, "same_sample": sample,
         "plain": c1,
         "batched_over_plain": round(value / world / c1["value"], 2),
+        "sequential": seq2,
+        "batched_over_sequential": round(value / world / seq2["value"], 2),
         "plain_c0": c0,
         "plain3d": p3,
         "batched3d": b3,
@@ -658,12 +667,17 @@ def plain3d(ctx, timed, iters, steps=16):
                         "jittered hexagonal lattice on z=0, " + C2_NOTE}
 
 
+def workload_batched3d():
+    """48 monolayers of N ~ U{8..64} cells at subdivision 3 (seeded)."""
+    from opencl_dpm_gb300 import clDPM
+    rng = np.random.default_rng(5)
+    return [build_monolayer(clDPM, rng, int(rng.integers(8, 65)), 3) for _ in range(48)]
+
+
 def batched3d(ctx, timed, iters, steps=16):
     """Many independent 3D monolayers in one batch: 48 tissues of N ~
     U{8..64} cells at subdivision 3, one launch per step for all of them."""
-    from opencl_dpm_gb300 import clDPM
-    rng = np.random.default_rng(5)
-    ts = [build_monolayer(clDPM, rng, int(rng.integers(8, 65)), 3) for _ in range(48)]
+    ts = workload_batched3d()
     b = make_batch3d(ctx, ts)
     for _ in range(3):
         b.step(steps, DT3)
@@ -674,6 +688,67 @@ def batched3d(ctx, timed, iters, steps=16):
             "vertices": int(b.nverts),
             "workload": "48 monolayers, N ~ U{8..64} cells x 642 vertices (subdivision 3), "
                         + C2_NOTE + ", one batch"}
+
+
+SEQ_HOW = ("the plain single-system path over the same tissues one after another: each "
+           "tissue alone as its own batch (2D: autotuned; small tissues take the resident "
+           "run), warmed, then timed without an L2 flush; the tissues' times are summed")
+
+
+def sequential_2d(ctx, timed, tissues):
+    """The batched sweep's tissues through the plain path, one at a time:
+    the summed time of one 32-step call per tissue."""
+    total = 0.0
+    for t in tissues:
+        b, _ = make_batch(ctx, [t])
+        b.autotune(DT, trial_blocks=2, use_cache=True)
+        b.step(SIM_STEPS, DT)
+        total += timed(3, lambda: b.step(SIM_STEPS, DT), flush=False)
+        b.close()
+    V = sum(int(np.sum(t["nv"])) for t in tissues)
+    return {"value": round(V * SIM_STEPS / total, 1), "unit": UNIT,
+            "ms_per_step": round(total * 1e3, 4), "sim_steps_per_step": SIM_STEPS,
+            "tissues": len(tissues), "how": SEQ_HOW}
+
+
+def sequential_3d(ctx, timed, ts, steps=16):
+    """The batched 3D leg's monolayers through the plain path, one at a time."""
+    total = 0.0
+    for t in ts:
+        b = make_batch3d(ctx, [t])
+        b.step(steps, DT3)
+        total += timed(3, lambda: b.step(steps, DT3), flush=False)
+        b.close()
+    V = sum(len(t["Kv"]) * t["nv"] for t in ts)
+    return {"value": round(V * steps / total, 1), "unit": UNIT,
+            "ms_per_step": round(total * 1e3, 4), "sim_steps_per_step": steps,
+            "tissues": len(ts), "how": SEQ_HOW}
+
+
+def service_time_alone(ctx, timed, t, sample_steps=256):
+    """Seconds per step of one served request's tissue alone on the plain
+    path (a batch of its own, warmed, `sample_steps` steps timed)."""
+    if t["dim"] == 2:
+        b, _ = make_batch(ctx, [t])
+        b.autotune(DT, trial_blocks=2, use_cache=True)
+        b.step(SIM_STEPS, DT)
+        s = timed(1, lambda: b.step(sample_steps, DT), flush=False)
+    else:
+        b = make_batch3d(ctx, [t])
+        b.step(16, DT3)
+        s = timed(1, lambda: b.step(sample_steps, DT3), flush=False)
+    b.close()
+    return s / sample_steps
+
+
+def fcfs(arrival, service):
+    """Completion times of requests served one at a time in arrival order."""
+    done = np.zeros(len(arrival))
+    free = 0.0
+    for i in np.argsort(arrival, kind="stable"):
+        free = max(free, arrival[i]) + service[i]
+        done[i] = free
+    return done
 
 
 def steady_state_leg(ctx, timed, geo, total=20000):
@@ -826,9 +901,12 @@ def served_capacity(ctx, seed, nreq=32, steps=2048):
     return vs / secs
 
 
-def run_served(ctx, nreq, plain2d, plain3d, seed=77):
+def run_served(ctx, timed, nreq, plain2d, plain3d, seed=77):
     """Seeded Poisson arrivals at 80% of the server's measured capacity for
-    this request mix; latency = completion - arrival (host clock)."""
+    this request mix; latency = completion - arrival (host clock).  Beside
+    it, the same requests at the same arrival times served one at a time on
+    the plain path: each request's tissue alone, its per-step time over 256
+    steps times its steps, queued first come first served."""
     reqs = served_requests(seed, nreq)
     cap = served_capacity(ctx, seed + 2)
     mean_vs = float(np.mean([t["verts"] * t["steps"] for t in reqs]))
@@ -877,6 +955,12 @@ def run_served(ctx, nreq, plain2d, plain3d, seed=77):
         return {"p50": round(float(np.percentile(x, 50)), 4),
                 "p99": round(float(np.percentile(x, 99)), 4)} if len(x) else None
 
+    per_step = np.array([service_time_alone(ctx, timed, t) for t in reqs])
+    service = per_step * np.array([t["steps"] for t in reqs], np.float64)
+    seq_done = fcfs(arrival, service)
+    seq_makespan = float(seq_done.max())
+    seq_lat = seq_done - arrival
+
     return {
         "value": round(vs / makespan, 1), "unit": UNIT,
         "by_dim": {"2d": {"value": round(vs2 / makespan, 1),
@@ -896,6 +980,17 @@ def run_served(ctx, nreq, plain2d, plain3d, seed=77):
         "vertex_steps": vs, "makespan_s": round(makespan, 3), "rounds": rounds,
         "arrival_rate_per_s": round(lam, 3),
         "capacity": round(cap, 1),
+        "sequential": {
+            "value": round(vs / seq_makespan, 1), "unit": UNIT,
+            "makespan_s": round(seq_makespan, 3),
+            "busy_s": round(float(service.sum()), 3),
+            "latency_s": {"p50": round(float(np.percentile(seq_lat, 50)), 4),
+                          "p99": round(float(np.percentile(seq_lat, 99)), 4)},
+            "served_over_sequential": round(seq_makespan / makespan, 2),
+            "capacity_over_sequential": round(cap / (vs / float(service.sum())), 2),
+            "how": "the same requests and arrival times served one at a time, first come first "
+                   "served, on the plain path: each request's tissue alone as its own batch, its "
+                   "per-step time over 256 timed steps times its steps"},
         "load": "arrival rate = 80% of the capacity measured first: the same server saturated "
                 "with 32 requests of this mix, 2,048 steps each",
         "pools": {"2d": [{"slots": s, "cells": c, "nv_max": 32} for s, c in POOLS_2D],
