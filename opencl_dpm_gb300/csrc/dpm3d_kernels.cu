@@ -86,15 +86,44 @@ __device__ float block_sum_v(const float (&v)[kSumThreads / NT], float *red) {
   for (int i = 0; i < kSumThreads / 32; ++i) t += red[i];
   return t;
 }
-template <int NT> __device__ float block_max(float v, float *red) {
-  v = warp_max(v);
+// NS block sums (each formed as block_sum_v forms it) and NM block maxima of
+// per-thread values in one pass: two barriers instead of two per value.
+// red holds 16 NS + (NT / 32) NM floats (at most 64).
+template <int NT, int NS, int NM>
+__device__ void block_reduce(const float (&sv)[NS][kSumThreads / NT], float (&so)[NS],
+                             const float (&mv)[NM], float (&mo)[NM], float *red) {
+  constexpr int R = kSumThreads / NT, VW = kSumThreads / 32, W = NT / 32;
+  static_assert(NS * VW + NM * W <= 64, "reduction scratch");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float ws[NS][R], wm[NM];
+#pragma unroll
+  for (int k = 0; k < NS; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) ws[k][r] = warp_sum(sv[k][r]);
+#pragma unroll
+  for (int k = 0; k < NM; ++k) wm[k] = warp_max(mv[k]);
   __syncthreads();
-  if (lane == 0) red[w] = v;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+#pragma unroll
+      for (int r = 0; r < R; ++r) red[k * VW + w + r * W] = ws[k][r];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) red[NS * VW + k * W + w] = wm[k];
+  }
   __syncthreads();
-  float r = -INFINITY;
-  for (int i = 0; i < NT / 32; ++i) r = fmaxf(r, red[i]);
-  return r;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    float t = 0.0f;
+    for (int i = 0; i < VW; ++i) t += red[k * VW + i];
+    so[k] = t;
+  }
+#pragma unroll
+  for (int k = 0; k < NM; ++k) {
+    float t = -INFINITY;
+    for (int i = 0; i < W; ++i) t = fmaxf(t, red[NS * VW + k * W + i]);
+    mo[k] = t;
+  }
 }
 
 // Centre of mass (sum times 1/NV, Cell3D_Kernel.cl:35-44), bounding radius
@@ -103,51 +132,53 @@ template <int NT, typename FaceIdx>
 __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, int nv,
                             const FaceIdx *faces, int nf, float *red) {
   constexpr int R = kSumThreads / NT;
-  float e2 = 0.f;
+  // pass 1: longest edge (maximum) and the vertex sums (centre)
+  float e2[1] = {0.f};
   for (int f = threadIdx.x; f < nf; f += NT) {
     const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
     const int a[3] = {i0, i1, i2}, b[3] = {i1, i2, i0};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const float dx = px[a[k]] - px[b[k]], dy = py[a[k]] - py[b[k]], dz = pz[a[k]] - pz[b[k]];
-      e2 = fmaxf(e2, dx * dx + dy * dy + dz * dz);
+      e2[0] = fmaxf(e2[0], dx * dx + dy * dy + dz * dz);
     }
   }
-  const float emax = sqrtf(block_max<NT>(e2, red));
-  float sx[R], sy[R], sz[R];
+  float sxyz[3][R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    sx[r] = sy[r] = sz[r] = 0.f;
+    sxyz[0][r] = sxyz[1][r] = sxyz[2][r] = 0.f;
     for (int v = threadIdx.x + r * NT; v < nv; v += kSumThreads) {
-      sx[r] += px[v];
-      sy[r] += py[v];
-      sz[r] += pz[v];
+      sxyz[0][r] += px[v];
+      sxyz[1][r] += py[v];
+      sxyz[2][r] += pz[v];
     }
   }
+  float sums[3], maxs[1];
+  block_reduce<NT, 3, 1>(sxyz, sums, e2, maxs, red);
   const float inv = 1.0f / (float)nv;
   Geom3D g;
-  g.cx = block_sum_v<NT>(sx, red) * inv;
-  g.cy = block_sum_v<NT>(sy, red) * inv;
-  g.cz = block_sum_v<NT>(sz, red) * inv;
-  float r2 = 0.f;
+  g.cx = sums[0] * inv;
+  g.cy = sums[1] * inv;
+  g.cz = sums[2] * inv;
+  g.emax = sqrtf(maxs[0]);
+  // pass 2: bounding radius and the inner ball.  With the centre as
+  // origin, face (a, b, c) has the triple product t = a.(b x c), whose sign
+  // is the sign of the reference's face term at the centre, and its plane
+  // lies |t| / |n| from the centre (n = (b - a) x (c - a)).  If every t has
+  // the same sign and the solid angles sum to less than 8 pi (each is at
+  // most area / plane distance^2), the mesh winds exactly once around the
+  // centre, and no face comes closer than the smallest plane distance, so
+  // the same holds in that ball.  (dmin is -1 once any face is degenerate,
+  // whatever the order.)
+  float mx[2] = {0.f, INFINITY};  // r2 and dmin (reduced as maxima of r2, -dmin)
   for (int v = threadIdx.x; v < nv; v += NT) {
     const float dx = px[v] - g.cx, dy = py[v] - g.cy, dz = pz[v] - g.cz;
-    r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+    mx[0] = fmaxf(mx[0], dx * dx + dy * dy + dz * dz);
   }
-  g.R = sqrtf(block_max<NT>(r2, red));
-  g.emax = emax;
-  // Inner ball.  With the centre as origin, face (a, b, c) has the triple
-  // product t = a.(b x c), whose sign is the sign of the reference's face
-  // term at the centre, and its plane lies |t| / |n| from the centre
-  // (n = (b - a) x (c - a)).  If every t has the same sign and the solid
-  // angles sum to less than 8 pi (each is at most area / plane distance^2),
-  // the mesh winds exactly once around the centre, and no face comes closer
-  // than the smallest plane distance, so the same holds in that ball.
-  // (dmin is -1 once any face is degenerate, whatever the order.)
-  float dmin = INFINITY, bound[R], npos[R];
+  float bn[2][R];  // bound, count of positive triple products
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    bound[r] = npos[r] = 0.f;
+    bn[0][r] = bn[1][r] = 0.f;
     for (int f = threadIdx.x + r * NT; f < nf; f += kSumThreads) {
       const int i0 = faces[3 * f], i1 = faces[3 * f + 1], i2 = faces[3 * f + 2];
       const f3 a = mk(px[i0] - g.cx, py[i0] - g.cy, pz[i0] - g.cz);
@@ -157,14 +188,17 @@ __device__ Geom3D mesh_geom(const float *px, const float *py, const float *pz, i
       const float nl = sqrtf(dot(n, n));
       const float t = dot(a, cross(b, c));
       const float d = fabsf(t) / nl;  // NaN or 0 for a degenerate face
-      dmin = d > 0.0f ? fminf(dmin, d) : -1.0f;
-      bound[r] += 0.5f * nl / (d * d);
-      npos[r] += t > 0.0f ? 1.0f : 0.0f;
+      mx[1] = d > 0.0f ? fminf(mx[1], d) : -1.0f;
+      bn[0][r] += 0.5f * nl / (d * d);
+      bn[1][r] += t > 0.0f ? 1.0f : 0.0f;
     }
   }
-  dmin = -block_max<NT>(-dmin, red);
-  const float bsum = block_sum_v<NT>(bound, red);
-  const float ns = block_sum_v<NT>(npos, red);
+  mx[1] = -mx[1];
+  float s2[2], m2[2];
+  block_reduce<NT, 2, 2>(bn, s2, mx, m2, red);
+  g.R = sqrtf(m2[0]);
+  const float dmin = -m2[1];
+  const float bsum = s2[0], ns = s2[1];
   const bool one_sign = ns == (float)nf || ns == 0.0f;
   const bool ok = one_sign && dmin > 0.0f && bsum < 8.0f * (float)M_PI * 0.999f;
   g.rin = ok ? dmin * (1.0f - 1e-4f) : 0.0f;
