@@ -832,7 +832,7 @@ SERVE_CHUNK = 256
 # subdivision level; slot memory is small next to HBM, so the pools are sized
 # for concurrency
 POOLS_2D = [(48, 128), (32, 512), (24, 2048)]
-POOLS_3D = [(16, 128)]
+POOLS_3D = [(8, 128), (8, 128)]  # two pools per mesh: their steps run side by side
 
 
 def served_requests(seed, nreq):

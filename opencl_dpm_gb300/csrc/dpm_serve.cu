@@ -129,16 +129,21 @@ int admit(dpm_server *s) {
       ++it;
       continue;
     }
-    // smallest fitting pool with a free slot
+    // smallest fitting pool with a free slot; among pools of the same
+    // shape, the one with the fewest requests (pools of one shape run side
+    // by side on their own streams, so spreading requests over them fills
+    // the GPU with more independent launches)
     int best = -1, slot = -1;
     for (int p = 0; p < (int)s->pools.size(); ++p) {
       Pool &P = s->pools[p];
       if (P.busy || !fits(P, *r)) continue;
       auto fs = std::find(P.slots.begin(), P.slots.end(), nullptr);
       if (fs == P.slots.end()) continue;
-      const bool smaller = best < 0 || P.cells_per_slot < s->pools[best].cells_per_slot ||
-                           (P.cells_per_slot == s->pools[best].cells_per_slot &&
-                            P.nv_max < s->pools[best].nv_max);
+      const Pool *B = best < 0 ? nullptr : &s->pools[best];
+      const bool smaller =
+          !B || P.cells_per_slot < B->cells_per_slot ||
+          (P.cells_per_slot == B->cells_per_slot &&
+           (P.nv_max < B->nv_max || (P.nv_max == B->nv_max && P.active < B->active)));
       if (smaller) {
         best = p;
         slot = (int)(fs - P.slots.begin());
