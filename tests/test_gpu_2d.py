@@ -133,6 +133,8 @@ def test_brute_force_path_matches(ctx):
     xy2, F2, fl2, *_ = check_case(ctx, s, 40, tuning=dict(rebuild_period=40, skin_rel=1e-6))
     assert np.array_equal(fl1, rflags) and np.array_equal(fl2, rflags)
     assert pos_err(xy1, rx) <= X_TOL and pos_err(xy2, rx) <= X_TOL
+    # the lists only prune: the rebuild period and skin change no bit
+    assert np.array_equal(xy1, xy2) and np.array_equal(F1, F2)
 
 
 def test_batched_equals_alone(ctx):

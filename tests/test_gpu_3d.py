@@ -182,6 +182,23 @@ def test_block_sizes_same_bits(ctx, level):
         b.set_block_threads(384)
 
 
+def test_tuning_same_bits_3d(ctx):
+    """The rebuild period and skin change only the neighbour lists, which
+    only prune: the same bits (a stale list falls back to the tissue scan)."""
+    s = make_tissue3d(6, level=2, phi0=0.5, seed=12)
+    out = []
+    for tuning in (dict(rebuild_period=1, skin_rel=1e-6), dict(rebuild_period=8, skin_rel=0.1),
+                   dict(rebuild_period=16, skin_rel=1e-6)):
+        b = gpu_batch3d(ctx, [s], tuning)
+        b.step(16, DT)
+        x, F = b.download()
+        out.append((x, F, b.winding()))
+    assert out[0][2].sum() > 0
+    for x, F, w in out[1:]:
+        assert np.array_equal(x, out[0][0]) and np.array_equal(F, out[0][1])
+        assert np.array_equal(w, out[0][2])
+
+
 def test_larger_mesh_after_smaller(ctx):
     """A batch of a larger mesh still steps after a batch of a smaller mesh
     was made (the step's shared-memory limit is shared by all batches)."""
