@@ -14,8 +14,10 @@ struct Step2DArgs {
   unsigned char *flags_out; // containment flags of this step, or nullptr
   const Geom2D *geom_in;    // geometry of pos_in
   Geom2D *geom_out;         // geometry of pos_out (written)
-  const Geom2D *geom0;      // geometry at the last neighbour-list rebuild
-  const int *nn;            // neighbour counts (kNbOverflow = scan tissue)
+  const Geom2D *geom0;      // geometry at the last neighbour-list rebuild (nullptr:
+                            // no lists, no staleness check)
+  const int *nn;            // neighbour counts (kNbOverflow = scan tissue; nullptr:
+                            // every cell scans its tissue)
   const int *nbr;           // neighbour lists, kMaxNB2D per cell
   int *stale;               // per tissue: list no longer covers all pairs
   int *err;                 // bit 0: non-finite positions

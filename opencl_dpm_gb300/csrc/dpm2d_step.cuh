@@ -116,7 +116,8 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
 
   // -- attraction and repulsion against the neighbour list (cells in
   // ascending order, as the reference loops over them).
-  const int nnc = a.nn[c];
+  // (nn null: no lists, every cell of the tissue is screened)
+  const int nnc = a.nn ? a.nn[c] : kNbOverflow;
   const bool scan_all =
       nnc == kNbOverflow || *((volatile const int *)(a.stale + tid)) != 0;
   const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
@@ -411,12 +412,17 @@ __device__ __forceinline__ void step_cell(const Step2DArgs &a, const int c, cons
   if (lane == 0) {
     a.geom_out[c] = g;
     if (!(isfinite(g.cx) && isfinite(g.cy) && isfinite(g.R))) atomicOr(a.err, 1);
-    const Geom2D g0 = a.geom0[c];
-    const float dc = sqrtf((g.cx - g0.cx) * (g.cx - g0.cx) + (g.cy - g0.cy) * (g.cy - g0.cy));
-    float d = dc + fmaxf(0.0f, g.R - g0.R);
-    d = fmaxf(d, fmaxf(fabsf(g.minx - g0.minx), fabsf(g.maxx - g0.maxx)));
-    d = fmaxf(d, fmaxf(fabsf(g.miny - g0.miny), fabsf(g.maxy - g0.maxy)));
-    if (!(d <= 0.5f * T.skin)) atomicOr(a.stale + tid, 1);
+    // the list stays valid while no cell moved more than skin/2 since the
+    // rebuild (no lists, geom0 null: the resident run scans every cell)
+    if (a.geom0) {
+      const Geom2D g0 = a.geom0[c];
+      const float dc =
+          sqrtf((g.cx - g0.cx) * (g.cx - g0.cx) + (g.cy - g0.cy) * (g.cy - g0.cy));
+      float d = dc + fmaxf(0.0f, g.R - g0.R);
+      d = fmaxf(d, fmaxf(fabsf(g.minx - g0.minx), fabsf(g.maxx - g0.maxx)));
+      d = fmaxf(d, fmaxf(fabsf(g.miny - g0.miny), fabsf(g.maxy - g0.maxy)));
+      if (!(d <= 0.5f * T.skin)) atomicOr(a.stale + tid, 1);
+    }
   }
 }
 
@@ -513,8 +519,8 @@ __global__ void __launch_bounds__(kResidentWarps * 32)
   Step2DArgs a = r.a;
   a.cells = cs;
   a.tissues = ts;
-  a.geom0 = r.a.geom0 + c0;
-  a.nn = r.a.nn + c0;
+  a.geom0 = nullptr;  // no lists: nothing to check or read
+  a.nn = nullptr;
   a.stale = &sh_stale;
   a.step_index = 0;
   a.order = nullptr;
