@@ -266,9 +266,9 @@ int dpm_serve_add_pool3d(dpm_server *s, int slots, int cells_per_slot, int nv, i
   P.dt = dt;
   P.faces.assign(faces, faces + 3 * (size_t)nf);
   if (int r = pool3d_create(s->ctx, slots, cells_per_slot, nv, nf, faces, &P.b3)) return r;
-  if (s->chunk % 8) {
+  if (s->chunk % 16) {
     dpm3d_destroy(P.b3);
-    return fail(DPM_EINVAL, "chunk_steps must be a multiple of 8 for 3D pools");
+    return fail(DPM_EINVAL, "chunk_steps must be a multiple of 16 for 3D pools");
   }
   if (cudaError_t e = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) {
     dpm3d_destroy(P.b3);
