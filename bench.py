@@ -20,7 +20,8 @@ time.
 
 Also reported (keys of the same line): the plain single-system paths -- the
 1,024-cell compression protocol ("plain"), the 16-cell run of 10,000 steps
-("plain_c0"), the 256-cell 3D monolayer ("plain3d") -- the sweep's own
+("plain_c0"), the 256-cell 3D monolayer ("plain3d", and "plain3d_sub2" at
+the reference's own 162-vertex mesh) -- the sweep's own
 tissues run one after another through the plain path ("sequential"; the
 same for the 3D batch and for the served requests), 48 monolayers in one
 batch ("batched3d"), the same 32-tissue sample the reference arm times
@@ -461,6 +462,7 @@ def run_ours(args, rank, world, local_rank):
     c1 = plain_c1(ctx, timed, geo)
     c0 = plain_c0(ctx, timed, geo)
     p3 = plain3d(ctx, timed, max(3, args.steps))
+    p3s2 = plain3d(ctx, timed, max(3, args.steps), level=2)
     b3 = batched3d(ctx, timed, max(3, args.steps))
     b3["batched_over_plain"] = round(b3["value"] / p3["value"], 2)
     seq2 = sequential_2d(ctx, timed, tissues)
@@ -492,6 +494,7 @@ def run_ours(args, rank, world, local_rank):
         "batched_over_sequential": round(value / world / seq2["value"], 2),
         "plain_c0": c0,
         "plain3d": p3,
+        "plain3d_sub2": p3s2,
         "batched3d": b3,
         "steady_state": steady,
         "disperse": disp,
@@ -652,19 +655,20 @@ def plain_c0(ctx, timed, geo, steps=10000):
             "tuning": tuned}
 
 
-def plain3d(ctx, timed, iters, steps=16):
+def plain3d(ctx, timed, iters, steps=16, level=3):
     """The plain 3D monolayer: 256 icospheres at subdivision 3 (642 vertices,
-    1,280 faces)."""
+    1,280 faces); at level 2, the reference's own mesh (162 vertices, 320
+    faces), the only one the reference can run."""
     from opencl_dpm_gb300 import clDPM
-    t = build_monolayer(clDPM, np.random.default_rng(3), 256, 3)
+    t = build_monolayer(clDPM, np.random.default_rng(3), 256, level)
     b = make_batch3d(ctx, [t])
     for _ in range(3):
         b.step(steps, DT3)
     secs = timed(iters, lambda: b.step(steps, DT3))
     return {"value": round(b.nverts * steps / secs, 1), "unit": UNIT,
             "ms_per_step": round(secs * 1e3, 4), "sim_steps_per_step": steps,
-            "workload": "1 monolayer, 256 cells x 642 vertices (icosphere subdivision 3), "
-                        "jittered hexagonal lattice on z=0, " + C2_NOTE}
+            "workload": f"1 monolayer, 256 cells x {t['nv']} vertices (icosphere subdivision "
+                        f"{level}), jittered hexagonal lattice on z=0, " + C2_NOTE}
 
 
 def workload_batched3d():
