@@ -58,10 +58,13 @@ __device__ __forceinline__ f3 cross(f3 a, f3 b) {
   return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 // normalize with the OpenCL special case: the zero vector maps to itself
+// (one reciprocal square root for the three components; within the parity
+// tolerance of the reference's divisions)
 __device__ __forceinline__ f3 normalize(f3 a) {
   const float l2 = dot(a, a);
   if (l2 == 0.0f) return a;
-  return a / sqrtf(l2);
+  const float r = rsqrtf(l2);
+  return mk(a.x * r, a.y * r, a.z * r);
 }
 
 // Block sum of per-thread partials, added as a kSumThreads-thread block
