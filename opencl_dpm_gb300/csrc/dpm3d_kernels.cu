@@ -230,9 +230,14 @@ constexpr int kNearList = 32;
 // of them (more are summed by their warp).
 constexpr int kDefer = 64;
 
-// Shared-memory layout of k3d_step (see step3d_smem_bytes).
+// Shared-memory layout of k3d_step (see step3d_smem_bytes).  The staged
+// neighbour (q*, pb), its candidate list and its geometry and centre (nbg, nbc)
+// exist twice: the repulsion works on one buffer while it fills the other
+// (staged_view selects one).
 struct Smem3D {
-  float4 *pb; // bounding sphere (centre, radius) of each patch of the neighbour
+  float4 *pb;  // bounding sphere (centre, radius) of each patch of the neighbour
+  Geom3D *nbg; // the neighbour's geometry
+  float4 *nbc; // the neighbour's centre, shifted to the image nearest this cell
   float *px, *py, *pz, *fx, *fy, *fz, *qx, *qy, *qz, *red;
   float *bnx, *bny, *bnz, *bnl, *bgx, *bgy, *bgz;
   int *ncand, *poff;
@@ -241,10 +246,21 @@ struct Smem3D {
   float *terms; // [2][nf] face terms of a deferred candidate
   float *ex, *ey, *ez, *eL; // unit vector (lower id -> higher id) and length of each edge
   unsigned char *wnc;
+  int qstride;  // floats from one staged buffer's q* to the other's
 };
 
+// Counters in Smem3D::ncand: the candidates of a neighbour and the next
+// candidate to take, each rotating over three neighbours (a counter is zeroed
+// one neighbour after its last read and two before its next write, with a
+// barrier on either side), and the deferred candidates of a neighbour,
+// alternating over two (the next neighbour's warps may add theirs while a
+// slow thread still reads this one's count).  That is the pipelined loop of
+// 512-thread blocks; the two-barrier loop of smaller blocks alternates the
+// first two candidate counters and uses the first deferred counter.
+constexpr int kCntCand = 0, kCntTake = 3, kCntDefer = 6, kNumCounters = 8;
+
 __host__ __device__ __forceinline__ int q_region(int nv, int nf, int ne) {
-  const int a = 3 * nv + 2 * nf, b = 4 * ne;
+  const int a = 6 * nv + 2 * nf, b = 4 * ne;
   return a > b ? a : b;
 }
 
@@ -252,7 +268,9 @@ template <int NT>
 __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool bend) {
   Smem3D s;
   s.pb = reinterpret_cast<float4 *>(base);
-  float *f = reinterpret_cast<float *>(s.pb + kMaxPatches3D);
+  s.nbg = reinterpret_cast<Geom3D *>(s.pb + 2 * kMaxPatches3D);
+  s.nbc = reinterpret_cast<float4 *>(s.nbg + 2);
+  float *f = reinterpret_cast<float *>(s.nbc + 2);
   s.px = f; f += nv;
   s.py = f; f += nv;
   s.pz = f; f += nv;
@@ -265,7 +283,8 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool
   s.qx = f;
   s.qy = f + nv;
   s.qz = f + 2 * nv;
-  s.terms = f + 3 * nv;
+  s.qstride = 3 * nv;
+  s.terms = f + 6 * nv;
   s.ex = f;
   s.ey = f + ne;
   s.ez = f + 2 * ne;
@@ -286,14 +305,14 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool
     s.bnx = s.bny = s.bnz = s.bnl = s.bgx = s.bgy = s.bgz = nullptr;
   }
   s.ncand = reinterpret_cast<int *>(f);
-  f += 4;
+  f += kNumCounters;
   s.poff = reinterpret_cast<int *>(f);
   f += kMaxPatches3D + 4;
   uint16_t *h = reinterpret_cast<uint16_t *>(f);
   s.faces = h;
   h += 3 * nf;
   s.cand = h;
-  h += nv;
+  h += 2 * nv;
   s.pvert = h;
   h += nv;
   s.nlist = h;
@@ -302,6 +321,20 @@ __device__ __forceinline__ Smem3D carve(char *base, int nv, int nf, int ne, bool
   h += kDefer;
   s.wnc = reinterpret_cast<unsigned char *>(h);
   return s;
+}
+
+// The view of s whose staged neighbour (q*, pb, cand, nbg, nbc) is buffer b.
+__device__ __forceinline__ Smem3D staged_view(const Smem3D &s, int b) {
+  Smem3D v = s;
+  const int o = b * s.qstride;
+  v.qx += o;
+  v.qy += o;
+  v.qz += o;
+  v.pb += b * kMaxPatches3D;
+  v.nbg += b;
+  v.nbc += b;
+  v.cand += b * (s.qstride / 3);
+  return v;
 }
 
 __device__ __forceinline__ f3 vtx(const Smem3D &s, int i) { return mk(s.px[i], s.py[i], s.pz[i]); }
@@ -686,7 +719,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k3d_step(Step3DArgs a) {
   const int NP = a.mesh.np;
   for (int i = tid; i < NV; i += NT) s.pvert[i] = a.mesh.pvert[i];
   if (tid <= NP) s.poff[tid] = a.mesh.poff[tid];
-  if (tid < 3) s.ncand[tid] = 0;
+  if (tid < kNumCounters) s.ncand[tid] = 0;
   __syncthreads();
 
   const Geom3D gi = a.geom_in[c];
@@ -832,92 +865,229 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k3d_step(Step3DArgs a) {
   }
   __syncthreads();
 
-  // RepellingForces (Cell3D_Kernel.cl:251-310) over the neighbour list
+  // RepellingForces (Cell3D_Kernel.cl:251-310) over the neighbour list.
+  // With 16 warps per cell (NT = 512) the neighbours within winding reach go
+  // through two staging buffers: the warps take the candidates of the
+  // neighbour in one buffer from a shared counter (one warp each; the first
+  // by warp index), and every thread, once the counter runs dry, compacts
+  // and stages its share of the next such neighbour into the other buffer;
+  // one barrier closes both.  With fewer warps (many small-mesh cells, four
+  // blocks per SM) each neighbour is staged, then its candidates taken in
+  // warp order, with a barrier after each phase: there the pipeline measured
+  // slower (4% on served pools of subdivision-2 requests).  Either way a
+  // vertex is a candidate of a neighbour at most once and its hits land
+  // neighbour by neighbour in list order (barriers separate them), so every
+  // vertex sums its forces in the reference's order and both loops give the
+  // same bits.
   if (T.Kre != 0.0f) {
     const int nnc = a.nn[c];
     const bool scan_all =
         nnc == kNbOverflow || *((volatile const int *)(a.stale + P.tissue)) != 0;
     const int count = scan_all ? (T.cell_end - T.cell_begin) : nnc;
     const int *list = a.nbr + (size_t)c * kMaxNB3D;
-    int par = 0;
-    for (int q = 0; q < count; ++q) {
-      const int j = scan_all ? T.cell_begin + q : list[q];
-      if (j == c) continue;
-      const Geom3D gj = a.geom_in[j];
-      const f3 shift = image_shift(gi, gj, T);
-      const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
-      const f3 dc = C - cj;
-      const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
-                        fabsf(C.z);
-      const float reach = winding_reach(gj);
-      const float rr = gi.R + reach + 1e-4f * (gi.R + reach) + 1e-5f * mag;
-      if (!(dot(dc, dc) <= rr * rr)) continue;
-      // candidate compaction and staging of the neighbour's mesh in one
-      // phase.  Two candidate counters alternate between neighbours: the
-      // one in use was zeroed during the previous neighbour's evaluation,
-      // when nobody reads it.
-      int *cnt = s.ncand + par;
-      const float rj = reach * (1.0f + 1e-4f) + 1e-5f * mag;
-      for (int v = tid; v < NV; v += NT) {
-        const f3 d = vtx(s, v) - cj;
-        if (dot(d, d) <= rj * rj) s.cand[atomicAdd(cnt, 1)] = (uint16_t)v;
-      }
-      stage_neighbour<NT>(s, a, j, shift, NV, NP, tid, w, lane);
-      __syncthreads();
-      const int ncand = *cnt;
-      if (tid == 0) s.ncand[par ^ 1] = 0;
-      par ^= 1;
-      if (ncand > 0) {
-        unsigned *nearm = s.near + w * kNearWords;
-        for (int i = w; i < ncand; i += kW) {
-          const int v = s.cand[i];
-          const f3 pt = vtx(s, v);
-          bool deferred;
-          float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                                s.nlist + w * kNearList, lane, true, deferred);
-          if (deferred) {
-            int slot = 0;
-            if (lane == 0) slot = atomicAdd(s.ncand + 2, 1);
-            slot = __shfl_sync(kFull, slot, 0);
-            if (slot < kDefer) {
-              if (lane == 0) s.defer[slot] = (uint16_t)v;
-              continue;
-            }
-            wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                            s.nlist + w * kNearList, lane, false, deferred);
-          }
-          if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
-          __syncwarp();
+    if constexpr (NT == 512) {
+      // the first listed neighbour at or after list position q whose winding
+      // reach meets this cell (count when there is none), with its id, its
+      // geometry and its shift to the periodic image nearest this cell
+      auto next_in_reach = [&](int q, int &j, Geom3D &gj, f3 &shift) {
+        for (; q < count; ++q) {
+          j = scan_all ? T.cell_begin + q : list[q];
+          if (j == c) continue;
+          gj = a.geom_in[j];
+          shift = image_shift(gi, gj, T);
+          const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
+          const f3 dc = C - cj;
+          const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
+                            fabsf(C.z);
+          const float reach = winding_reach(gj);
+          const float rr = gi.R + reach + 1e-4f * (gi.R + reach) + 1e-5f * mag;
+          if (dot(dc, dc) <= rr * rr) return q;
         }
-      }
+        return count;
+      };
+      // this thread's share of neighbour k (id j) in buffer b: the candidate
+      // vertices within its winding reach, its staged mesh and patch spheres,
+      // its geometry and shifted centre
+      auto fill = [&](int b, int k, int j, const Geom3D &gj, f3 shift) {
+        const Smem3D sb = staged_view(s, b);
+        const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
+        const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
+                          fabsf(C.z);
+        const float rj = winding_reach(gj) * (1.0f + 1e-4f) + 1e-5f * mag;
+        int *cnt = s.ncand + kCntCand + k % 3;
+        for (int v = tid; v < NV; v += NT) {
+          const f3 d = vtx(s, v) - cj;
+          if (dot(d, d) <= rj * rj) sb.cand[atomicAdd(cnt, 1)] = (uint16_t)v;
+        }
+        stage_neighbour<NT>(sb, a, j, shift, NV, NP, tid, w, lane);
+        if (tid == 0) {
+          sb.nbg[0] = gj;
+          sb.nbc[0] = make_float4(cj.x, cj.y, cj.z, 0.0f);
+        }
+      };
+      int j = 0;
+      Geom3D gn;
+      f3 shift;
+      int q = next_in_reach(0, j, gn, shift);
+      if (q < count) fill(0, 0, j, gn, shift);
       __syncthreads();
-      // the deferred candidates, one after the other: the block evaluates
-      // the face terms into a buffer, then one warp adds them up in the
-      // order of the warp-level sum (lane l: faces l, l + 32, ...; then
-      // the butterfly), so the result is the one that warp would give;
-      // two buffers let that warp add while the block evaluates the next
-      const int nd = min(s.ncand[2], kDefer);
-      for (int d = 0; d < nd; ++d) {
-        float *tb = s.terms + (d & 1) * NF;
-        const int v = s.defer[d];
-        const f3 pt = vtx(s, v);
-        for (int f = tid; f < NF; f += NT) {
-          float num, denom;
-          face_term(s, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num, denom);
-          tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
+      for (int k = 0; q < count; ++k) {
+        const Smem3D sb = staged_view(s, k & 1);
+        const int ncand = s.ncand[kCntCand + k % 3];
+        // the counters of neighbour k - 1: read before the last barrier,
+        // written next for neighbour k + 2 after the coming one
+        if (tid == 0) {
+          s.ncand[kCntCand + (k + 2) % 3] = 0;
+          s.ncand[kCntTake + (k + 2) % 3] = 0;
+        }
+        if (ncand > 0) {
+          const Geom3D &gj = sb.nbg[0];
+          const float4 c4 = sb.nbc[0];
+          const f3 cj = mk(c4.x, c4.y, c4.z);
+          unsigned *nearm = s.near + w * kNearWords;
+          int *take = s.ncand + kCntTake + k % 3;
+          bool first = true;
+          for (;;) {
+            int i = w;
+            if (!first) {
+              if (lane == 0) i = kW + atomicAdd(take, 1);
+              i = __shfl_sync(kFull, i, 0);
+            }
+            first = false;
+            if (i >= ncand) break;
+            const int v = sb.cand[i];
+            const f3 pt = vtx(s, v);
+            bool deferred;
+            float wn = winding_at(sb, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
+                                  s.nlist + w * kNearList, lane, true, deferred);
+            if (deferred) {
+              int slot = 0;
+              if (lane == 0) slot = atomicAdd(s.ncand + kCntDefer + (k & 1), 1);
+              slot = __shfl_sync(kFull, slot, 0);
+              if (slot < kDefer) {
+                if (lane == 0) s.defer[slot] = (uint16_t)v;
+                continue;
+              }
+              wn = winding_at(sb, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
+                              s.nlist + w * kNearList, lane, false, deferred);
+            }
+            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+            __syncwarp();
+          }
+        }
+        const int qn = next_in_reach(q + 1, j, gn, shift);
+        if (qn < count) fill((k + 1) & 1, k + 1, j, gn, shift);
+        __syncthreads();
+        // the deferred candidates, one after the other: the block evaluates
+        // the face terms into a buffer, then one warp adds them up in the
+        // order of the warp-level sum (lane l: faces l, l + 32, ...; then
+        // the butterfly), so the result is the one that warp would give;
+        // two buffers let that warp add while the block evaluates the next
+        const int nd = min(s.ncand[kCntDefer + (k & 1)], kDefer);
+        for (int d = 0; d < nd; ++d) {
+          float *tb = s.terms + (d & 1) * NF;
+          const int v = s.defer[d];
+          const f3 pt = vtx(s, v);
+          for (int f = tid; f < NF; f += NT) {
+            float num, denom;
+            face_term(sb, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num,
+                      denom);
+            tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
+          }
+          __syncthreads();
+          if (tid == 0 && d == nd - 1) s.ncand[kCntDefer + (k & 1)] = 0;
+          if (w == d % kW) {
+            float part = 0.0f;
+            for (int f = lane; f < NF; f += 32) part += tb[f];
+            const float wn = warp_sum(part) / (4.0f * (float)M_PI);
+            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+          }
+        }
+        // the last deferred hit lands before the next neighbour's hits
+        if (nd > 0) __syncthreads();
+        q = qn;
+      }
+    } else {
+      int par = 0;
+      for (int q = 0; q < count; ++q) {
+        const int j = scan_all ? T.cell_begin + q : list[q];
+        if (j == c) continue;
+        const Geom3D gj = a.geom_in[j];
+        const f3 shift = image_shift(gi, gj, T);
+        const f3 cj = mk(gj.cx + shift.x, gj.cy + shift.y, gj.cz + shift.z);
+        const f3 dc = C - cj;
+        const float mag = fabsf(cj.x) + fabsf(cj.y) + fabsf(cj.z) + fabsf(C.x) + fabsf(C.y) +
+                          fabsf(C.z);
+        const float reach = winding_reach(gj);
+        const float rr = gi.R + reach + 1e-4f * (gi.R + reach) + 1e-5f * mag;
+        if (!(dot(dc, dc) <= rr * rr)) continue;
+        // candidate compaction and staging of the neighbour's mesh (buffer
+        // 0) in one phase.  Two candidate counters alternate between
+        // neighbours: the one in use was zeroed during the previous
+        // neighbour's evaluation, when nobody reads it.
+        int *cnt = s.ncand + kCntCand + par;
+        const float rj = reach * (1.0f + 1e-4f) + 1e-5f * mag;
+        for (int v = tid; v < NV; v += NT) {
+          const f3 d = vtx(s, v) - cj;
+          if (dot(d, d) <= rj * rj) s.cand[atomicAdd(cnt, 1)] = (uint16_t)v;
+        }
+        stage_neighbour<NT>(s, a, j, shift, NV, NP, tid, w, lane);
+        __syncthreads();
+        const int ncand = *cnt;
+        if (tid == 0) s.ncand[kCntCand + (par ^ 1)] = 0;
+        par ^= 1;
+        if (ncand > 0) {
+          unsigned *nearm = s.near + w * kNearWords;
+          for (int i = w; i < ncand; i += kW) {
+            const int v = s.cand[i];
+            const f3 pt = vtx(s, v);
+            bool deferred;
+            float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
+                                  s.nlist + w * kNearList, lane, true, deferred);
+            if (deferred) {
+              int slot = 0;
+              if (lane == 0) slot = atomicAdd(s.ncand + kCntDefer, 1);
+              slot = __shfl_sync(kFull, slot, 0);
+              if (slot < kDefer) {
+                if (lane == 0) s.defer[slot] = (uint16_t)v;
+                continue;
+              }
+              wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
+                              s.nlist + w * kNearList, lane, false, deferred);
+            }
+            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+            __syncwarp();
+          }
         }
         __syncthreads();
-        if (tid == 0 && d == nd - 1) s.ncand[2] = 0;
-        if (w == d % kW) {
-          float part = 0.0f;
-          for (int f = lane; f < NF; f += 32) part += tb[f];
-          const float wn = warp_sum(part) / (4.0f * (float)M_PI);
-          if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+        // the deferred candidates, one after the other: the block evaluates
+        // the face terms into a buffer, then one warp adds them up in the
+        // order of the warp-level sum (lane l: faces l, l + 32, ...; then
+        // the butterfly), so the result is the one that warp would give;
+        // two buffers let that warp add while the block evaluates the next
+        const int nd = min(s.ncand[kCntDefer], kDefer);
+        for (int d = 0; d < nd; ++d) {
+          float *tb = s.terms + (d & 1) * NF;
+          const int v = s.defer[d];
+          const f3 pt = vtx(s, v);
+          for (int f = tid; f < NF; f += NT) {
+            float num, denom;
+            face_term(s, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num, denom);
+            tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
+          }
+          __syncthreads();
+          if (tid == 0 && d == nd - 1) s.ncand[kCntDefer] = 0;
+          if (w == d % kW) {
+            float part = 0.0f;
+            for (int f = lane; f < NF; f += 32) part += tb[f];
+            const float wn = warp_sum(part) / (4.0f * (float)M_PI);
+            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+          }
         }
       }
+      // the last deferred sum's force lands after the loop's last barrier
+      __syncthreads();
     }
-    // the last deferred sum's force lands after the loop's last barrier
-    __syncthreads();
   }
 
   // AllVertAttraction (Cell3D_Kernel.cl:313-364), opt-in (Kat != 0): after
@@ -1304,9 +1474,9 @@ __global__ void __launch_bounds__(kNb3Warps * 32) k3d_neighbors(Rebuild3DArgs a,
 size_t step3d_smem_bytes(int nv, int nf, int ne, bool bend, int threads) {
   const size_t warps = (size_t)threads / 32;
   size_t floats = (size_t)6 * nv + (size_t)q_region(nv, nf, ne) + 64 + warps * kNearWords +
-                  (bend ? (size_t)7 * nf : 0) + 4 + kMaxPatches3D + 4;
-  size_t halves = (size_t)3 * nf + 2 * (size_t)nv + warps * kNearList + kDefer;
-  return sizeof(float4) * kMaxPatches3D + floats * 4 + halves * 2 + (size_t)nv + 16;
+                  (bend ? (size_t)7 * nf : 0) + kNumCounters + kMaxPatches3D + 4;
+  size_t halves = (size_t)3 * nf + 3 * (size_t)nv + warps * kNearList + kDefer;
+  return sizeof(float4) * (2 * kMaxPatches3D + 6) + floats * 4 + halves * 2 + (size_t)nv + 16;
 }
 
 int step3d_threads(int nv, int nf, int ne, bool bend, int ncells, int sm_count) {
