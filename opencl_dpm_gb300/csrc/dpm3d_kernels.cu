@@ -1485,7 +1485,7 @@ int step3d_threads(int nv, int nf, int ne, bool bend, int ncells, int sm_count) 
   // threads let four cells share an SM when their shared memory fits in its
   // 228 KB (1 KB reserved per block).  Measured on subdivision-2 batches of
   // 1,660-2,048 cells: 256 threads 14-17% faster; on 64-256 cells, or at
-  // subdivision 3 (96 KB per block), 512 faster.
+  // subdivision 3 (98 KB per block), 512 faster.
   const size_t b256 = step3d_smem_bytes(nv, nf, ne, bend, 256) + 1024;
   const bool four_fit = 4 * b256 <= (size_t)228 * 1024;
   return four_fit && ncells > 2 * sm_count ? 256 : 512;
