@@ -151,6 +151,34 @@ def test_monolayer_level3_contacts(ctx):
 
 
 @pytest.mark.parametrize("level", [2, 3])
+def test_dense_overlap_block_sizes_same_bits(ctx, level):
+    """Strongly overlapping cells (packing fraction 0.8 in the reference's
+    box rule, random centres): each cell has many neighbours within winding
+    reach and many vertices lie inside a neighbour.  512-thread blocks run
+    the neighbour pipeline (two staging buffers, candidates from a shared
+    counter), 256 and 128 threads the two-barrier loop: the same bits, and
+    the same as the oracle within the parity criteria."""
+    s = make_tissue3d(20, level=level, phi0=0.8, seed=40 + level, Kb=0.05, adh=0.1)
+    out = {}
+    for threads in (512, 256, 128):
+        b = gpu_batch3d(ctx, [s])
+        b.set_block_threads(threads)
+        b.step(5, DT)
+        x, F = b.download()
+        out[threads] = (x, F, b.winding())
+    x0, F0, w0 = out[512]
+    assert w0.sum() > 200  # many hits
+    for threads in (256, 128):
+        x, F, w = out[threads]
+        assert np.array_equal(x, x0) and np.array_equal(F, F0), threads
+        assert np.array_equal(w, w0), threads
+    x, F, wn, rx, rF, rwn = run_case(ctx, s, 1)
+    assert wn_ok(wn, rwn)[0], wn_ok(wn, rwn)
+    assert rel_norm_err(F, rF) <= F_TOL
+    assert pos_err(x, rx) <= X_TOL
+
+
+@pytest.mark.parametrize("level", [2, 3])
 def test_block_sizes_same_bits(ctx, level):
     """128, 256 and 512 threads per cell (and the default) give the same
     bits: every block-wide sum is formed in the 512-thread order.  A
