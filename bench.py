@@ -515,9 +515,14 @@ def sweep_config(ntissues, ncells, nverts):
 
 def step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info):
     """HBM and issue rooflines of the fused step kernel (k2d_step)."""
-    # one launch at a time after an L2 flush (cold), and launches as they run
-    # inside a graph: one rebuild period of step launches queued back to back
-    # after a fresh neighbour-list rebuild, warm, timed together
+    # one launch at a time after an L2 flush (cold); one rebuild period of
+    # step launches queued back to back after a fresh neighbour-list rebuild
+    # (warm, without the graph: each launch forks the vertex-slot classes
+    # over two streams by events); and the step launches' share of the graph
+    # replays: the same call timed (L2 flushed, as the headline) at the tuned
+    # rebuild period and at half of it, whose difference is the extra
+    # rebuilds inside the graph; the headline call less its rebuilds is the
+    # step launches' time
     nk = 20
     kern = timed(nk, lambda: b.step_kernel(DT))
     period = tuned["rebuild_period"]
@@ -527,7 +532,19 @@ def step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info):
             b.step_kernel(DT)
 
     b.rebuild_now()
-    in_graph = timed(1, period_of_steps, flush=False) / period
+    back_to_back = timed(1, period_of_steps, flush=False) / period
+    call = lambda: b.step(SIM_STEPS, DT)
+    rebuild, in_graph, t_full = None, back_to_back, None
+    if period % 4 == 0 and SIM_STEPS % period == 0:
+        t_full = timed(10, call)
+        b.set_tuning(rebuild_period=period // 2)
+        call()  # captures the graph of the shorter period
+        t_half = timed(10, call)
+        b.set_tuning(rebuild_period=period)
+        call()
+        n_full, n_half = SIM_STEPS // period, SIM_STEPS // (period // 2)
+        rebuild = (t_half - t_full) / (n_half - n_full)
+        in_graph = (ms_per_step / 1e3 - n_full * rebuild) / SIM_STEPS
     bytes_per_launch = 16.0 * V + 28.0 * N
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_per_launch / in_graph / 1e9
@@ -546,8 +563,16 @@ def step_roofline(b, timed, V, N, ms_per_step, tuned, clock_info):
             "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS)",
             "kernel": "k2d_step (one launch per vertex-slot class, together)",
             "in_graph_us": round(in_graph * 1e6, 2),
-            "in_graph_how": "a rebuild period of step launches queued back to back after a "
-                            "rebuild, warm (the graph's launches without the graph)",
+            "in_graph_how": "one call of 32 steps timed again (L2 flushed) at the tuned "
+                            "rebuild period and at half of it: the difference per extra rebuild "
+                            "is rebuild_us; (headline ms_per_step - its rebuilds) / 32 is the "
+                            "step launches' time inside the graph",
+            "rebuild_us": None if rebuild is None else round(rebuild * 1e6, 2),
+            "call_retimed_ms": None if t_full is None else round(t_full * 1e3, 4),
+            "back_to_back_us": round(back_to_back * 1e6, 2),
+            "back_to_back_how": "a rebuild period of step launches queued back to back after a "
+                                "rebuild, warm, without the graph (each launch forks the "
+                                "vertex-slot classes over two streams by events)",
             "cold_single_launch_us": round(kern * 1e6, 2),
             "cold_frac": round(bytes_per_launch / kern / 1e9 / peak, 4),
             "bytes_per_launch": int(bytes_per_launch),
