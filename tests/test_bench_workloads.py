@@ -48,3 +48,36 @@ print(json.dumps(line))
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["config"]["workload"] and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_roofline_rows_of_the_committed_profile():
+    """The bench line's roofline takes the step kernel's DRAM traffic, warp
+    instructions per launch and the captured build from the committed ncu
+    summary; the rows must parse, and the traffic must be close to the
+    algorithmic bytes of one step of the sweep (16 B per vertex and 28 B per
+    cell: no re-reads)."""
+    import bench
+    rows = bench.profile_rows("k2d_step_batched512")
+    assert rows["build"] and rows["traffic"] and rows["warp_inst"]
+    V, N = 1940768, 66116
+    algorithmic = 16.0 * V + 28.0 * N
+    assert 0.9 <= rows["traffic"] / algorithmic <= 1.2
+    assert 1e7 < rows["warp_inst"] < 1e9
+
+
+def test_launches_per_call_counts_each_class_and_rebuild():
+    """gpu_launches: per rebuild period one bin-preparation, three per radix
+    pass and one neighbour-list launch; per simulation step one step launch
+    per vertex-slot class."""
+    import bench
+
+    class FakeBatch:
+        ntissues = 512
+
+        def bins(self):
+            return 9, None, None, None
+
+    tissues = [{"nv": np.full(4, nv)} for nv in (16, 24, 32, 48)]
+    assert bench.slot_classes(tissues) == 2
+    passes = (9 + 9 + 7) // 8
+    assert bench.launches_per_call(FakeBatch(), tissues, 32, 32) == (1 + 3 * passes + 1) + 64
