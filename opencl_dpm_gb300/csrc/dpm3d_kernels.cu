@@ -683,6 +683,64 @@ __device__ __forceinline__ void attract_pair(f3 p, f3 q, float L0i, float L0j, f
   }
 }
 
+// One winding candidate v of the staged neighbour (view sb: its mesh,
+// centre cj and geometry gj), decided by one warp: the hit lands on v's
+// force, or v is queued in sb.defer (counter *ndefer) for the block-wide
+// full sum after the neighbour's other candidates (beyond kDefer of them
+// the warp sums every face itself).
+__device__ __forceinline__ void decide_candidate(const Smem3D &sb, const Mesh3D &m, int NV,
+                                                 int NF, int NP, int v, f3 cj,
+                                                 const Geom3D &gj, f3 C, float Kre,
+                                                 unsigned *nearm, uint16_t *nlist, int lane,
+                                                 int *ndefer) {
+  const f3 pt = vtx(sb, v);
+  bool deferred;
+  float wn = winding_at(sb, m, NV, NF, NP, pt, cj, gj, nearm, nlist, lane, true, deferred);
+  if (deferred) {
+    int slot = 0;
+    if (lane == 0) slot = atomicAdd(ndefer, 1);
+    slot = __shfl_sync(kFull, slot, 0);
+    if (slot < kDefer) {
+      if (lane == 0) sb.defer[slot] = (uint16_t)v;
+      return;
+    }
+    wn = winding_at(sb, m, NV, NF, NP, pt, cj, gj, nearm, nlist, lane, false, deferred);
+  }
+  if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(sb, v, wn, C, pt, Kre);
+}
+
+// The deferred candidates of the staged neighbour (view sb), one after the
+// other: the block evaluates the face terms into a buffer, then one warp
+// adds them up in the order of the warp-level sum (lane l: faces l, l + 32,
+// ...; then the butterfly), so the result is the one that warp would give;
+// two buffers let that warp add while the block evaluates the next.  The
+// counter is zeroed after its last read.  Returns how many were summed (the
+// last one's hit lands after the last barrier here).
+template <int NT>
+__device__ __forceinline__ int deferred_sums(const Smem3D &sb, int NF, int *ndefer, f3 C,
+                                             float Kre, int tid, int w, int lane) {
+  const int nd = min(*ndefer, kDefer);
+  for (int d = 0; d < nd; ++d) {
+    float *tb = sb.terms + (d & 1) * NF;
+    const int v = sb.defer[d];
+    const f3 pt = vtx(sb, v);
+    for (int f = tid; f < NF; f += NT) {
+      float num, denom;
+      face_term(sb, sb.faces[3 * f], sb.faces[3 * f + 1], sb.faces[3 * f + 2], pt, num, denom);
+      tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
+    }
+    __syncthreads();
+    if (tid == 0 && d == nd - 1) *ndefer = 0;
+    if (w == d % (NT / 32)) {
+      float part = 0.0f;
+      for (int f = lane; f < NF; f += 32) part += tb[f];
+      const float wn = warp_sum(part) / (4.0f * (float)M_PI);
+      if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(sb, v, wn, C, pt, Kre);
+    }
+  }
+  return nd;
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) k3d_step(Step3DArgs a) {
   constexpr int kW = NT / 32;  // warps per cell
@@ -955,54 +1013,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k3d_step(Step3DArgs a) {
             }
             first = false;
             if (i >= ncand) break;
-            const int v = sb.cand[i];
-            const f3 pt = vtx(s, v);
-            bool deferred;
-            float wn = winding_at(sb, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                                  s.nlist + w * kNearList, lane, true, deferred);
-            if (deferred) {
-              int slot = 0;
-              if (lane == 0) slot = atomicAdd(s.ncand + kCntDefer + (k & 1), 1);
-              slot = __shfl_sync(kFull, slot, 0);
-              if (slot < kDefer) {
-                if (lane == 0) s.defer[slot] = (uint16_t)v;
-                continue;
-              }
-              wn = winding_at(sb, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                              s.nlist + w * kNearList, lane, false, deferred);
-            }
-            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+            decide_candidate(sb, a.mesh, NV, NF, NP, sb.cand[i], cj, gj, C, T.Kre, nearm,
+                             s.nlist + w * kNearList, lane, s.ncand + kCntDefer + (k & 1));
             __syncwarp();
           }
         }
         const int qn = next_in_reach(q + 1, j, gn, shift);
         if (qn < count) fill((k + 1) & 1, k + 1, j, gn, shift);
         __syncthreads();
-        // the deferred candidates, one after the other: the block evaluates
-        // the face terms into a buffer, then one warp adds them up in the
-        // order of the warp-level sum (lane l: faces l, l + 32, ...; then
-        // the butterfly), so the result is the one that warp would give;
-        // two buffers let that warp add while the block evaluates the next
-        const int nd = min(s.ncand[kCntDefer + (k & 1)], kDefer);
-        for (int d = 0; d < nd; ++d) {
-          float *tb = s.terms + (d & 1) * NF;
-          const int v = s.defer[d];
-          const f3 pt = vtx(s, v);
-          for (int f = tid; f < NF; f += NT) {
-            float num, denom;
-            face_term(sb, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num,
-                      denom);
-            tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
-          }
-          __syncthreads();
-          if (tid == 0 && d == nd - 1) s.ncand[kCntDefer + (k & 1)] = 0;
-          if (w == d % kW) {
-            float part = 0.0f;
-            for (int f = lane; f < NF; f += 32) part += tb[f];
-            const float wn = warp_sum(part) / (4.0f * (float)M_PI);
-            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
-          }
-        }
+        const int nd = deferred_sums<NT>(sb, NF, s.ncand + kCntDefer + (k & 1), C, T.Kre, tid,
+                                         w, lane);
         // the last deferred hit lands before the next neighbour's hits
         if (nd > 0) __syncthreads();
         q = qn;
@@ -1039,51 +1059,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k3d_step(Step3DArgs a) {
         if (ncand > 0) {
           unsigned *nearm = s.near + w * kNearWords;
           for (int i = w; i < ncand; i += kW) {
-            const int v = s.cand[i];
-            const f3 pt = vtx(s, v);
-            bool deferred;
-            float wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                                  s.nlist + w * kNearList, lane, true, deferred);
-            if (deferred) {
-              int slot = 0;
-              if (lane == 0) slot = atomicAdd(s.ncand + kCntDefer, 1);
-              slot = __shfl_sync(kFull, slot, 0);
-              if (slot < kDefer) {
-                if (lane == 0) s.defer[slot] = (uint16_t)v;
-                continue;
-              }
-              wn = winding_at(s, a.mesh, NV, NF, NP, pt, cj, gj, nearm,
-                              s.nlist + w * kNearList, lane, false, deferred);
-            }
-            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
+            decide_candidate(s, a.mesh, NV, NF, NP, s.cand[i], cj, gj, C, T.Kre, nearm,
+                             s.nlist + w * kNearList, lane, s.ncand + kCntDefer);
             __syncwarp();
           }
         }
         __syncthreads();
-        // the deferred candidates, one after the other: the block evaluates
-        // the face terms into a buffer, then one warp adds them up in the
-        // order of the warp-level sum (lane l: faces l, l + 32, ...; then
-        // the butterfly), so the result is the one that warp would give;
-        // two buffers let that warp add while the block evaluates the next
-        const int nd = min(s.ncand[kCntDefer], kDefer);
-        for (int d = 0; d < nd; ++d) {
-          float *tb = s.terms + (d & 1) * NF;
-          const int v = s.defer[d];
-          const f3 pt = vtx(s, v);
-          for (int f = tid; f < NF; f += NT) {
-            float num, denom;
-            face_term(s, s.faces[3 * f], s.faces[3 * f + 1], s.faces[3 * f + 2], pt, num, denom);
-            tb[f] = denom < 1e-8f ? 0.0f : 2.0f * atan2f(num, denom);
-          }
-          __syncthreads();
-          if (tid == 0 && d == nd - 1) s.ncand[kCntDefer] = 0;
-          if (w == d % kW) {
-            float part = 0.0f;
-            for (int f = lane; f < NF; f += 32) part += tb[f];
-            const float wn = warp_sum(part) / (4.0f * (float)M_PI);
-            if (lane == 0 && !(fabsf(wn) < 1e-6f)) repel(s, v, wn, C, pt, T.Kre);
-          }
-        }
+        deferred_sums<NT>(s, NF, s.ncand + kCntDefer, C, T.Kre, tid, w, lane);
       }
       // the last deferred sum's force lands after the loop's last barrier
       __syncthreads();
